@@ -1,0 +1,341 @@
+"""Benchmark of the GB300 block step.
+
+Workload (default): the synthetic tsunami at 2048 x 2048 cells as 4 x 4 blocks
+of 512^2 (100 km box, b = -2000 + 500 sin cos + seeded noise, Gaussian bump),
+HLLE solver, unsplit step (the path swe_benchmark_mpi runs), global time
+stepping.  One bench step = one time step (ghost layer + fluxes/dt + update)
+of the whole domain.  Metric: cell-updates/s (higher is better).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+gb300 arm: state resident in HBM; L2 (126 MB) is flushed by writing 256 MB
+between timed steps (the 2048^2 state, 67 MB, would otherwise stay in L2);
+each step is timed with CUDA events on the library's stream.  `e2e` runs the
+same steps through the C ABI on host buffers: upload h, hu, hv, b from pinned
+memory, step, download h, hu, hv, timed on the host clock.  `roofline` is the
+fused update kernel's algorithmic bytes (28 B/cell) over its event-timed
+duration; `cpu_baseline` times the oracle (CPU restatement of the reference's
+algorithm) on the host cores for a bounded sample of the same workload.
+reference arm: the oracle on all host cores (the reference's own compiled
+code cannot run on the GPU host: its solver module is absent and its
+sources are not shipped), one bounded sample per step.
+Multi-GPU: replicas only (independent copies, no collective in the step);
+value = all ranks' cell updates / max-over-ranks time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for p in (os.path.join(ROOT, "swe-ppm_gb300"), os.path.join(ROOT, "oracle")):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+N_CELLS_SIDE = 2048
+N_BLOCKS = 16
+SEED = 20261203
+BYTES_PER_CELL = 28  # read h, hu, hv, b; write h, hu, hv (FP32)
+METRIC = "cell-updates/s at 2048^2 (plain fused path, HLLE, unsplit step)"
+PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def workload_config(extra=None):
+    cfg = {"workload": "synthetic tsunami 2048x2048 as 4x4 blocks of 512^2, HLLE, unsplit step, GTS",
+           "cells": N_CELLS_SIDE * N_CELLS_SIDE, "blocks": "4x4", "block_cells": "512x512", "solver": "hlle",
+           "semantics": "unsplit (SWE_DimensionalSplittingMpi)", "seed": SEED,
+           "l2": "flushed between timed steps (256 MB write)"}
+    if extra:
+        cfg.update(extra)
+    return cfg
+
+
+def peaks():
+    try:
+        with open(PEAKS_PATH) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+                out = ""
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def setup_domain(swe, device):
+    geo, h, hu, hv, b = swe.init_domain(swe.SCENARIO_TSUNAMI, N_CELLS_SIDE, N_CELLS_SIDE, N_BLOCKS,
+                                        [N_CELLS_SIDE, SEED, 100000.0])
+    tile_rows = int(os.environ.get("SWE_TILE_ROWS", "0"))
+    tile_cols = int(os.environ.get("SWE_TILE_COLS", "0"))
+    D = swe.Domain(geo["nx_cols"], geo["ny_rows"], geo["dx"], geo["dy"], boundary=geo["boundary"], solver=swe.HLLE,
+                   tile_rows=tile_rows, tile_cols=tile_cols, device=device)
+    D.upload(h, hu, hv, b)
+    D.exchange_bathymetry()
+    return D, geo, (h, hu, hv, b)
+
+
+def cpu_baseline(seconds=12.0):
+    """The oracle on all host cores (one OpenMP thread per block), a bounded
+    number of steps of the same 2048^2 workload."""
+    import oracle
+    import swe_gb300 as swe
+    oracle.build()
+    geo, h, hu, hv, b = swe.init_domain(swe.SCENARIO_TSUNAMI, N_CELLS_SIDE, N_CELLS_SIDE, N_BLOCKS,
+                                        [N_CELLS_SIDE, SEED, 100000.0])
+    R = oracle.Domain(geo["nx_cols"], geo["ny_rows"], geo["dx"], geo["dy"], outer=geo["boundary"], solver=oracle.HLLE)
+    R.set_state(h, hu, hv, b)
+    R.bathymetry_ghosts()
+    t0 = time.perf_counter()
+    _, threads = R.step_parallel(1)  # also calibrates
+    t1 = time.perf_counter()
+    per = max(t1 - t0, 1e-3)
+    n = max(1, min(200, int(seconds / per)))
+    t0 = time.perf_counter()
+    R.step_parallel(n)
+    el = time.perf_counter() - t0
+    cells = N_CELLS_SIDE * N_CELLS_SIDE
+    return {"value": cells * n / el, "unit": "cell-updates/s", "cores": int(threads), "kind": "port",
+            "sample": "%d steps of the 2048^2 workload (oracle, OpenMP over 16 blocks), %.1f s" % (n, el),
+            "seconds_per_step": el / n}
+
+
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if os.environ.get("SWE_BENCH_BACKEND", "") != "gloo" else "gloo"
+        dist.init_process_group(backend=backend)
+    return world, rank, local
+
+
+def dist_max(v, world):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(v)], dtype=torch.float64,
+                     device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def dist_barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return 0
+    steps = []
+    base = None
+    for i in range(args.warmup + args.steps):
+        b = cpu_baseline(seconds=float(os.environ.get("SWE_REF_SECONDS", "8")))
+        if i >= args.warmup:
+            steps.append(b["value"])
+        base = b
+    value = statistics.median(steps)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * base["seconds_per_step"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded tsunami scenario)", "config": workload_config({"parallelism": "host cores"}),
+            "cpu_baseline": {"value": value, "unit": "cell-updates/s", "cores": base["cores"], "kind": base["kind"],
+                             "sample": base["sample"]},
+            "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gb300(args, world, rank, local):
+    import torch
+    import swe_gb300 as swe
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    D, geo, host = setup_domain(swe, local)
+    stream = torch.cuda.current_stream(dev)
+    D.set_stream(stream.cuda_stream)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    cells = N_CELLS_SIDE * N_CELLS_SIDE
+
+    def one_step():
+        D.set_ghost_layer()
+        D.compute_fluxes()
+        D.update_unknowns()
+
+    for _ in range(max(args.warmup, 3)):
+        flush.zero_()
+        one_step()
+    torch.cuda.synchronize(dev)
+    dist_barrier(world)
+
+    # timed region: K steps, L2 flushed before each, CUDA events around each step
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize(dev)
+        dist_barrier(world)
+        for i in range(args.steps):
+            flush.zero_()
+            starts[i].record(stream)
+            one_step()
+            ends[i].record(stream)
+        torch.cuda.synchronize(dev)
+        dist_barrier(world)
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_ms = dist_max(sum(step_ms), world)
+    ms_per_step = total_ms / args.steps
+
+    # per-kernel breakdown (same region shape, events between the three launches)
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
+    for i in range(args.steps):
+        flush.zero_()
+        ev[i][0].record(stream)
+        D.set_ghost_layer()
+        ev[i][1].record(stream)
+        D.compute_fluxes()
+        ev[i][2].record(stream)
+        D.update_unknowns()
+        ev[i][3].record(stream)
+    torch.cuda.synchronize(dev)
+    t_ghost = statistics.mean(e[0].elapsed_time(e[1]) for e in ev)
+    t_speed = statistics.mean(e[1].elapsed_time(e[2]) for e in ev)
+    t_update = statistics.mean(e[2].elapsed_time(e[3]) for e in ev)
+    status = D.status()
+
+    # end to end through the C ABI on host buffers (pinned)
+    pinned = [torch.from_numpy(a).pin_memory() for a in host]
+    outs = [torch.empty(host[0].shape, dtype=torch.float32).pin_memory() for _ in range(3)]
+    pn = [p.numpy() for p in pinned]
+    on = [o.numpy() for o in outs]
+    e2e_steps = max(3, min(args.steps, 10))
+    D.set_stream(None)
+    for _ in range(2):
+        D.upload(*pn)
+        D.step(1)
+        D.download_into(on)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        D.upload(*pn)
+        D.step(1)
+        D.download_into(on)
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    e2e_s = dist_max(e2e_s, world)
+    h2d = sum(p.nbytes for p in pn)
+    d2h = sum(o.nbytes for o in on)
+
+    hbm, peak_kind = peaks()
+    algo_bytes = BYTES_PER_CELL * cells
+    achieved = algo_bytes / (t_update * 1e-3) / 1e9
+    step_achieved = algo_bytes / (ms_per_step * 1e-3) / 1e9
+    traffic = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            traffic = json.load(f).get("update_kernel_dram_bytes")
+    except Exception:
+        pass
+
+    base = cpu_baseline(float(os.environ.get("SWE_CPU_BASELINE_SECONDS", "12"))) if rank == 0 else None
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": world * cells / (ms_per_step * 1e-3), "unit": "cell-updates/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded tsunami scenario, shapes of the 2048^2 benchmark)",
+            "config": workload_config({"parallelism": "replicas x%d" % world if world > 1 else "1 GPU"}),
+            "roofline": {"bound": "hbm", "kernel": "sweepKernel<HLLE,unsplit,update>", "achieved": achieved,
+                         "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "peak_kind": peak_kind,
+                         "traffic": traffic, "algorithmic_bytes_per_launch": algo_bytes,
+                         "step_achieved": step_achieved, "step_frac": step_achieved / hbm},
+            "kernel_ms": {"ghost": t_ghost, "speed": t_speed, "update": t_update},
+            "cpu_baseline": {k: base[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "e2e": {"value": world * cells / e2e_s, "unit": "cell-updates/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "clocks": clk.summary(), "gpu_launches": 3 * args.steps, "device_status": status,
+        }
+        print(json.dumps(line), flush=True)
+    D.close()
+    dist_barrier(world)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    args = ap.parse_args()
+    world, rank, local = dist_init()
+    if args.impl == "reference":
+        rc = run_reference(args, world, rank)
+    else:
+        rc = run_gb300(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return rc
+
+
+if __name__ == "__main__":
+    sys.exit(main())

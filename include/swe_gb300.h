@@ -1,0 +1,156 @@
+/*
+ * swe_gb300.h -- C ABI of the GB300 block step of the SWE-PPM finite-volume
+ * shallow-water solver.
+ *
+ * Plain C: pointers, sizes and ints only; every function returns an int
+ * status (0 = OK, negative = error, message via swe_gpu_last_error()); no
+ * exception crosses the ABI.  One domain handle owns a set of blocks in one
+ * device allocation plus a CUDA stream; calls on distinct handles are
+ * thread-safe, a single handle is not re-entrant.
+ *
+ * The entry points replace the reference's block interface:
+ *   SWE_Block<T, Buffer>                      src/blocks/SWE_Block.hh:110-251
+ *   SWE_DimensionalSplittingMpi               src/blocks/SWE_DimensionalSplittingMpi.hh:52-124
+ *   SWE_DimensionalSplittingMPIOverdecomp     src/blocks/SWE_DimensionalSplittingMPIOverdecomp.hh:50-117
+ *   SWE_DimensionalSplitting (serial)         src/blocks/SWE_DimensionalSplitting.hh:41-83
+ *   solver::{FWave,AugRie,HLLEFun,Hybrid}<float>::computeNetUpdates
+ *                                             (call sites src/blocks/SWE_DimensionalSplittingMpi.cpp:403-410)
+ * Block arrays use the reference's Float2D layout: a[x][y] = raw[x*ld + y]
+ * with ld >= ny+2 (src/tools/Float2D.hh:74-80), ghost ring at 0 and n+1.
+ */
+#ifndef SWE_GB300_H
+#define SWE_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SWE_GPU_OK 0
+#define SWE_GPU_ERR_INVALID (-1)   /* bad argument or handle */
+#define SWE_GPU_ERR_CUDA (-2)      /* CUDA runtime error */
+#define SWE_GPU_ERR_DEVICE (-3)    /* device-side status flag set (e.g. NaN wave speed) */
+#define SWE_GPU_ERR_NOMEM (-4)     /* device allocation failed */
+
+/* Riemann solvers.  The reference chooses at compile time with
+ * WAVE_PROPAGATION_SOLVER (SConstruct:543-553, src/blocks/SWE_DimensionalSplittingMpi.hh:42-50):
+ * 0 "hybrid" = HLLEFun in the distributed blocks and Hybrid in the serial
+ * block, 1 = FWave, 2 = AugRie.  Here the choice is a runtime value. */
+#define SWE_SOLVER_FWAVE 1
+#define SWE_SOLVER_AUGRIE 2
+#define SWE_SOLVER_HYBRID 3
+#define SWE_SOLVER_HLLE 4
+
+/* step semantics: UNSPLIT = SWE_DimensionalSplittingMpi / ...MPIOverdecomp
+ * (src/blocks/SWE_DimensionalSplittingMpi.cpp:383-518), SPLIT = serial
+ * SWE_DimensionalSplitting (src/blocks/SWE_DimensionalSplitting.cpp:105-210) */
+#define SWE_SEMANTICS_UNSPLIT 0
+#define SWE_SEMANTICS_SPLIT 1
+
+/* how the split block reduces its x wave speed: MAX = max over all x-edges;
+ * LAST_EDGE = the reference's one-thread result (the solver overwrites the
+ * reduction variable, src/blocks/SWE_DimensionalSplitting.cpp:118-131) */
+#define SWE_SPLIT_DT_MAX 0
+#define SWE_SPLIT_DT_LAST_EDGE 1
+
+/* BoundaryType values of src/types/Boundary.hh:23-30 */
+#define SWE_OUTFLOW 0
+#define SWE_WALL 1
+#define SWE_INFLOW 2
+#define SWE_CONNECT 3
+#define SWE_CONNECT_WITHIN_RANK 4
+#define SWE_PASSIVE 5
+
+/* Boundary index values of src/types/Boundary.hh:5-10 */
+#define SWE_BND_LEFT 0
+#define SWE_BND_RIGHT 1
+#define SWE_BND_BOTTOM 2
+#define SWE_BND_TOP 3
+
+typedef struct swe_gpu_domain swe_gpu_domain;
+
+/* A blocks_x x blocks_y grid of blocks (one simulation, global time step):
+ * the overdecomposed layout of src/examples/swe_mpi_overdecomp.cpp:148-225.
+ * Block k sits at (k / blocks_y, k % blocks_y) like rank k in
+ * src/examples/swe_mpi.cpp:186-187; neighbours get CONNECT_WITHIN_RANK, outer
+ * sides `boundary[]`. */
+typedef struct swe_gpu_desc {
+    int blocks_x, blocks_y;
+    const int *nx_cols;  /* blocks_x interior widths */
+    const int *ny_rows;  /* blocks_y interior heights */
+    float dx, dy;
+    int boundary[4];     /* outer boundary types, indexed LEFT, RIGHT, BOTTOM, TOP */
+    int solver;          /* SWE_SOLVER_* */
+    int semantics;       /* SWE_SEMANTICS_* */
+    int split_dt_mode;   /* SWE_SPLIT_DT_* (split semantics only) */
+    int tile_rows;       /* rows per CTA (multiple of 32, <= 256); 0 = default */
+    int tile_cols;       /* columns per x-chunk (<= 128); 0 = default */
+    int device;          /* CUDA device ordinal */
+} swe_gpu_desc;
+
+int swe_gpu_domain_create(const swe_gpu_desc *desc, swe_gpu_domain **out);
+int swe_gpu_domain_destroy(swe_gpu_domain *dom);
+int swe_gpu_block_count(const swe_gpu_domain *dom, int *count);
+int swe_gpu_block_shape(const swe_gpu_domain *dom, int block, int *nx, int *ny);
+
+/* Copies one block's state (incl. ghosts) from host arrays in Float2D layout
+ * with column stride `ld` floats; NULL skips a field.  Replaces writing the
+ * block's h/hu/hv/b (SWE_Block::getModifiable*, src/blocks/SWE_Block.hh:130-142). */
+int swe_gpu_upload_block(swe_gpu_domain *dom, int block, const float *h, const float *hu, const float *hv,
+                         const float *b, int ld);
+/* Copies one block's current state to host arrays; returns when the data is there
+ * (SWE_Block::getWaterHeight & co., src/blocks/SWE_Block.hh:128-142). */
+int swe_gpu_download_block(swe_gpu_domain *dom, int block, float *h, float *hu, float *hv, float *b, int ld);
+
+/* bathymetry ghosts: OUTFLOW/WALL copies (SWE_Block::applyBoundaryBathymetry,
+ * src/blocks/SWE_Block.hh:724-749) and neighbour copies (exchangeBathymetry,
+ * src/blocks/SWE_DimensionalSplittingMpi.cpp:109-186; sendBathymetry,
+ * src/blocks/SWE_DimensionalSplittingMPIOverdecomp.cpp:208-266) */
+int swe_gpu_exchange_bathymetry(swe_gpu_domain *dom);
+
+/* setGhostLayer (src/blocks/SWE_DimensionalSplittingMpi.cpp:188-376): boundary
+ * conditions and on-device halo copies between blocks */
+int swe_gpu_set_ghost_layer(swe_gpu_domain *dom);
+/* computeNumericalFluxes (src/blocks/SWE_DimensionalSplittingMpi.cpp:383-476):
+ * wave speeds of every edge and the group's maxTimestep, kept on the device */
+int swe_gpu_compute_fluxes(swe_gpu_domain *dom);
+/* updateUnknowns (src/blocks/SWE_DimensionalSplittingMpi.cpp:484-518); like the
+ * reference it applies the maxTimestep of the preceding compute_fluxes and
+ * ignores `dt` */
+int swe_gpu_update_unknowns(swe_gpu_domain *dom, float dt);
+/* getMaxTimestep (src/blocks/SWE_Block.hh:594-597); synchronises */
+int swe_gpu_get_max_timestep(swe_gpu_domain *dom, float *dt);
+
+/* `nsteps` fused steps (ghosts + fluxes + update) queued on the stream; no host
+ * synchronisation */
+int swe_gpu_step(swe_gpu_domain *dom, int nsteps);
+/* the drivers' checkpoint loop `while (t < t_end) { step; t += dt; }`
+ * (src/examples/swe_mpi.cpp:300-327) run on the device from a captured CUDA
+ * graph; returns the executed steps and the float time reached */
+int swe_gpu_advance(swe_gpu_domain *dom, float t_end, int max_steps, int *steps_done, float *t_now);
+int swe_gpu_get_time(swe_gpu_domain *dom, float *t, int *steps);
+int swe_gpu_set_time(swe_gpu_domain *dom, float t);
+
+int swe_gpu_sync(swe_gpu_domain *dom);
+/* device-side status bits (bit 0: NaN wave speed); 0 when healthy */
+int swe_gpu_status(swe_gpu_domain *dom, int *status);
+/* the CUDA stream the handle launches on (a cudaStream_t) */
+int swe_gpu_get_stream(swe_gpu_domain *dom, void **stream);
+/* launch on a caller's CUDA stream (a cudaStream_t of the handle's device,
+ * e.g. a framework's current stream); NULL returns to the handle's own stream */
+int swe_gpu_set_stream(swe_gpu_domain *dom, void *stream);
+/* message of the last failed call on this thread */
+const char *swe_gpu_last_error(void);
+int swe_gpu_version(void);
+
+/* Per-edge solver on device arrays (solver::X<float>::computeNetUpdates over n
+ * edges): inputs hL, hR, huL, huR, bL, bR; outputs hUpdL, hUpdR, huUpdL,
+ * huUpdR, maxWaveSpeed.  All pointers are device memory; `stream` may be NULL. */
+int swe_gpu_solve_edges(int solver, long long n, const float *hL, const float *hR, const float *huL,
+                        const float *huR, const float *bL, const float *bR, float *hUpdL, float *hUpdR,
+                        float *huUpdL, float *huUpdR, float *maxWaveSpeed, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

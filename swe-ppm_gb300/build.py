@@ -1,0 +1,81 @@
+"""Builds the library in-tree: swe-ppm_gb300/_build/libswe_gb300.so.
+
+CUDA sources are compiled for sm_103a only (one -gencode), in parallel, with
+-fmad=false (every fused multiply-add in the kernels is an explicit fmaf) and
+IEEE division / square root, so the kernels reproduce the CPU restatement bit
+for bit.  Host C++ (scenarios, initialisation, writer) is compiled with g++
+-ffp-contract=off and linked into the same shared library.
+"""
+import os
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+OUT = os.path.join(HERE, "_build")
+LIB = os.path.join(OUT, "libswe_gb300.so")
+
+CUDA_SOURCES = ["csrc/swe_capi.cu", "csrc/swe_kernels_fh.cu", "csrc/swe_kernels_aug.cu"]
+HOST_SOURCES = ["host/swe_host.cpp"]
+NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-fmad=false", "-lineinfo", "-std=c++17",
+              "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-I" + os.path.join(ROOT, "include")]
+CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-I" + os.path.join(ROOT, "include"),
+             "-I" + os.path.join(HERE, "host")]
+
+
+def _nvcc():
+    for cand in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", "nvcc"):
+        if cand and (os.path.isabs(cand) and os.path.exists(cand) or not os.path.isabs(cand)):
+            return cand
+    return "nvcc"
+
+
+def _stale(target, deps):
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def _deps():
+    out = []
+    for sub in ("csrc", "host"):
+        d = os.path.join(HERE, sub)
+        out += [os.path.join(d, f) for f in os.listdir(d)]
+    out.append(os.path.join(ROOT, "include", "swe_gb300.h"))
+    return out
+
+
+def build(verbose=False, force=False):
+    os.makedirs(OUT, exist_ok=True)
+    deps = _deps()
+    if not force and not _stale(LIB, deps):
+        return LIB
+    nvcc = _nvcc()
+    jobs = []
+    objs = []
+    for src in CUDA_SOURCES:
+        obj = os.path.join(OUT, os.path.basename(src) + ".o")
+        objs.append(obj)
+        jobs.append([nvcc] + NVCC_FLAGS + ["-c", os.path.join(HERE, src), "-o", obj])
+    for src in HOST_SOURCES:
+        obj = os.path.join(OUT, os.path.basename(src) + ".o")
+        objs.append(obj)
+        jobs.append(["g++"] + CXX_FLAGS + ["-c", os.path.join(HERE, src), "-o", obj])
+
+    def run(cmd):
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if verbose or r.returncode:
+            sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)
+        if r.returncode:
+            raise RuntimeError("compilation failed: " + " ".join(cmd))
+
+    with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
+        list(ex.map(run, jobs))
+    run([nvcc, "-shared", "-o", LIB] + objs + ["-lcudart"])
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(verbose="-v" in sys.argv, force="-f" in sys.argv))

@@ -1,0 +1,580 @@
+// C ABI of the GB300 block step (include/swe_gb300.h): domain set-up, state
+// transfer, the ghost-layer and bathymetry kernels, and the step drivers.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/swe_gb300.h"
+#include "swe_device.cuh"
+#include "swe_launch.hpp"
+
+using namespace swegb;
+
+namespace {
+
+thread_local std::string g_lastError;
+
+int fail(int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_lastError = buf;
+    return code;
+}
+
+#define CUDA_TRY(call)                                                                            \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess) return fail(SWE_GPU_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// setGhostLayer: boundary conditions (src/blocks/SWE_Block.hh:757-911) and the
+// intra-rank copies of the neighbours' copy layers
+// (src/blocks/SWE_DimensionalSplittingMPIOverdecomp.cpp:273-304).  One thread
+// per ghost cell of one block (blockIdx.y); reads touch only interior cells,
+// writes only ghost cells, so blocks never race.
+// ---------------------------------------------------------------------------
+__global__ void ghostKernel(const DomainDev d, int bathymetry) {
+    const BlockDesc B = d.blocks[blockIdx.y];
+    const GroupState *G = d.groups + B.group;
+    if (!bathymetry && !(*((volatile const float *)&G->time) < *((volatile const float *)&G->target))) return;
+    const int cur = G->cur;
+    const int nx = B.nx, ny = B.ny;
+    const size_t P = size_t(B.pitch);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    float *fields[3];
+    int nf;
+    if (bathymetry) {
+        fields[0] = d.b;
+        nf = 1;
+    } else {
+        fields[0] = cur ? d.h[1] : d.h[0];
+        fields[1] = cur ? d.hu[1] : d.hu[0];
+        fields[2] = cur ? d.hv[1] : d.hv[0];
+        nf = 3;
+    }
+    int side, pos;
+    if (i < ny) { side = 0; pos = i + 1; }
+    else if (i < 2 * ny) { side = 1; pos = i - ny + 1; }
+    else if (i < 2 * ny + nx) { side = 2; pos = i - 2 * ny + 1; }
+    else if (i < 2 * ny + 2 * nx) { side = 3; pos = i - 2 * ny - nx + 1; }
+    else if (i < 2 * ny + 2 * nx + 4) { side = 4; pos = i - 2 * ny - 2 * nx; }
+    else return;
+
+    if (side == 4) {  // corners from the diagonal interior cell
+        const int gx = (pos & 1) ? nx + 1 : 0, gy = (pos & 2) ? ny + 1 : 0;
+        const int sx = (pos & 1) ? nx : 1, sy = (pos & 2) ? ny : 1;
+        for (int f = 0; f < nf; f++) {
+            float *F = fields[f] + B.base;
+            F[size_t(gx) * P + gy] = F[size_t(sx) * P + sy];
+        }
+        return;
+    }
+    const int type = B.bnd[side];
+    // ghost cell and its source inside this block
+    int gx, gy, sx, sy, negate;
+    switch (side) {
+    case 0: gx = 0; gy = pos; sx = 1; sy = pos; negate = 1; break;
+    case 1: gx = nx + 1; gy = pos; sx = nx; sy = pos; negate = 1; break;
+    case 2: gx = pos; gy = 0; sx = pos; sy = 1; negate = 2; break;
+    default: gx = pos; gy = ny + 1; sx = pos; sy = ny; negate = 2; break;
+    }
+    long long srcBase = B.base;
+    size_t srcP = P;
+    if (type == CONNECT_WITHIN_RANK) {
+        const BlockDesc N = d.blocks[B.nbr[side]];
+        srcBase = N.base;
+        srcP = size_t(N.pitch);
+        switch (side) {
+        case 0: sx = N.nx; break;
+        case 1: sx = 1; break;
+        case 2: sy = N.ny; break;
+        default: sy = 1; break;
+        }
+        negate = 0;
+    } else if (type == OUTFLOW) {
+        negate = 0;
+    } else if (type != WALL) {
+        return;  // CONNECT, INFLOW, PASSIVE: set elsewhere
+    }
+    if (bathymetry) negate = 0;
+    for (int f = 0; f < nf; f++) {
+        const float v = fields[f][srcBase + size_t(sx) * srcP + sy];
+        fields[f][B.base + size_t(gx) * P + gy] = (negate == f && f > 0) ? -v : v;
+    }
+}
+
+/// per-edge solver over arrays (solver::X<float>::computeNetUpdates)
+template <int S>
+__global__ void solveEdgesKernel(long long n, const float *hL, const float *hR, const float *huL, const float *huR,
+                                 const float *bL, const float *bR, float *oHL, float *oHR, float *oHuL, float *oHuR,
+                                 float *oS) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float a = hL[i], c = hR[i], e = huL[i], f = huR[i];
+    Cell L, R;
+    L.h = a; L.hn = e; L.b = bL[i];
+    R.h = c; R.hn = f; R.b = bR[i];
+    L.u = (a < kDryTol) ? 0.f : e / a;
+    R.u = (c < kDryTol) ? 0.f : f / c;
+    L.sq = sqrtf(a); R.sq = sqrtf(c);
+    L.c = sqrtf(kG * a); R.c = sqrtf(kG * c);
+    edgeSolve<S>(L, R, oHL[i], oHR[i], oHuL[i], oHuR[i], oS[i]);
+}
+
+} // namespace
+
+struct swe_gpu_domain {
+    int device = 0;
+    cudaStream_t stream = nullptr;     // stream launches go to
+    cudaStream_t ownStream = nullptr;  // the handle's own stream
+    int solver = SOLVER_HLLE, semantics = SEM_UNSPLIT, splitDtMode = SPLIT_DT_MAX;
+    int tileRows = 256, tileCols = 32;
+    std::vector<BlockDesc> blocks;
+    std::vector<WorkUnit> units;
+    std::vector<GroupState> groupsInit;
+    int ngroups = 1;
+    int maxPerimeter = 0;
+    size_t fieldElems = 0;
+    float *h[2] = {nullptr, nullptr}, *hu[2] = {nullptr, nullptr}, *hv[2] = {nullptr, nullptr}, *b = nullptr;
+    BlockDesc *dBlocks = nullptr;
+    WorkUnit *dUnits = nullptr;
+    GroupState *dGroups = nullptr;
+    DomainDev dev{};
+    cudaGraphExec_t graph = nullptr;
+    int graphSteps = 0;
+};
+
+namespace {
+
+int enqueueGhost(swe_gpu_domain *D, int bathymetry) {
+    const int threads = 128;
+    dim3 grid((D->maxPerimeter + threads - 1) / threads, unsigned(D->blocks.size()));
+    ghostKernel<<<grid, threads, 0, D->stream>>>(D->dev, bathymetry);
+    CUDA_TRY(cudaGetLastError());
+    return SWE_GPU_OK;
+}
+
+int enqueueSpeed(swe_gpu_domain *D) {
+    CUDA_TRY(launchSpeed(D->dev, int(D->units.size()), D->tileRows, D->stream));
+    return SWE_GPU_OK;
+}
+
+int enqueueUpdate(swe_gpu_domain *D) {
+    CUDA_TRY(launchUpdate(D->dev, int(D->units.size()), D->tileRows, D->stream));
+    return SWE_GPU_OK;
+}
+
+int enqueueStep(swe_gpu_domain *D) {
+    int rc = enqueueGhost(D, 0);
+    if (rc) return rc;
+    rc = enqueueSpeed(D);
+    if (rc) return rc;
+    return enqueueUpdate(D);
+}
+
+int readGroups(swe_gpu_domain *D, std::vector<GroupState> &g) {
+    g.resize(D->ngroups);
+    CUDA_TRY(cudaStreamSynchronize(D->stream));
+    CUDA_TRY(cudaMemcpy(g.data(), D->dGroups, sizeof(GroupState) * D->ngroups, cudaMemcpyDeviceToHost));
+    return SWE_GPU_OK;
+}
+
+int setTargets(swe_gpu_domain *D, float target) {
+    for (int g = 0; g < D->ngroups; g++)
+        CUDA_TRY(cudaMemcpyAsync(&D->dGroups[g].target, &target, sizeof(float), cudaMemcpyHostToDevice, D->stream));
+    CUDA_TRY(cudaStreamSynchronize(D->stream));
+    return SWE_GPU_OK;
+}
+
+void freeDomain(swe_gpu_domain *D) {
+    if (D->graph) cudaGraphExecDestroy(D->graph);
+    for (int i = 0; i < 2; i++) {
+        cudaFree(D->h[i]);
+        cudaFree(D->hu[i]);
+        cudaFree(D->hv[i]);
+    }
+    cudaFree(D->b);
+    cudaFree(D->dBlocks);
+    cudaFree(D->dUnits);
+    cudaFree(D->dGroups);
+    if (D->ownStream) cudaStreamDestroy(D->ownStream);
+    delete D;
+}
+
+int checkBlock(const swe_gpu_domain *D, int block) {
+    if (!D) return fail(SWE_GPU_ERR_INVALID, "null domain handle");
+    if (block < 0 || block >= int(D->blocks.size()))
+        return fail(SWE_GPU_ERR_INVALID, "block %d out of range [0, %d)", block, int(D->blocks.size()));
+    return SWE_GPU_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+const char *swe_gpu_last_error(void) { return g_lastError.c_str(); }
+
+int swe_gpu_version(void) { return 1; }
+
+int swe_gpu_domain_create(const swe_gpu_desc *desc, swe_gpu_domain **out) {
+    if (!desc || !out) return fail(SWE_GPU_ERR_INVALID, "null descriptor or output pointer");
+    *out = nullptr;
+    const int bx = desc->blocks_x, by = desc->blocks_y;
+    if (bx < 1 || by < 1 || !desc->nx_cols || !desc->ny_rows)
+        return fail(SWE_GPU_ERR_INVALID, "need at least one block and the block sizes");
+    if (!(desc->dx > 0.f) || !(desc->dy > 0.f)) return fail(SWE_GPU_ERR_INVALID, "dx, dy must be positive");
+    if (desc->solver < SWE_SOLVER_FWAVE || desc->solver > SWE_SOLVER_HLLE)
+        return fail(SWE_GPU_ERR_INVALID, "unknown solver %d", desc->solver);
+    if (desc->semantics != SWE_SEMANTICS_UNSPLIT && desc->semantics != SWE_SEMANTICS_SPLIT)
+        return fail(SWE_GPU_ERR_INVALID, "unknown semantics %d", desc->semantics);
+    if (desc->semantics == SWE_SEMANTICS_SPLIT && bx * by != 1)
+        return fail(SWE_GPU_ERR_INVALID, "the split step is defined for a single block");
+    for (int i = 0; i < 4; i++)
+        if (desc->boundary[i] < SWE_OUTFLOW || desc->boundary[i] > SWE_PASSIVE)
+            return fail(SWE_GPU_ERR_INVALID, "unknown boundary type %d", desc->boundary[i]);
+    for (int i = 0; i < bx; i++)
+        if (desc->nx_cols[i] < 1) return fail(SWE_GPU_ERR_INVALID, "block width must be >= 1");
+    for (int i = 0; i < by; i++)
+        if (desc->ny_rows[i] < 1) return fail(SWE_GPU_ERR_INVALID, "block height must be >= 1");
+    int tileRows = desc->tile_rows > 0 ? desc->tile_rows : 256;
+    int tileCols = desc->tile_cols > 0 ? desc->tile_cols : 32;
+    if (tileRows % 32 != 0 || tileRows > kMaxTileRows) return fail(SWE_GPU_ERR_INVALID, "tile_rows must be a multiple of 32 <= %d", kMaxTileRows);
+    if (tileCols > kMaxTileCols) return fail(SWE_GPU_ERR_INVALID, "tile_cols must be <= %d", kMaxTileCols);
+
+    auto *D = new swe_gpu_domain();
+    D->device = desc->device;
+    D->solver = desc->solver;
+    D->semantics = desc->semantics;
+    D->splitDtMode = desc->split_dt_mode;
+    int maxNy = 0;
+    for (int i = 0; i < by; i++) maxNy = std::max(maxNy, desc->ny_rows[i]);
+    D->tileRows = std::min(tileRows, ((maxNy + 31) / 32) * 32);
+    D->tileCols = tileCols;
+
+    cudaError_t e = cudaSetDevice(D->device);
+    if (e != cudaSuccess) {
+        delete D;
+        return fail(SWE_GPU_ERR_CUDA, "cudaSetDevice(%d): %s", desc->device, cudaGetErrorString(e));
+    }
+    e = cudaStreamCreateWithFlags(&D->ownStream, cudaStreamNonBlocking);
+    D->stream = D->ownStream;
+    if (e != cudaSuccess) {
+        delete D;
+        return fail(SWE_GPU_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
+    }
+
+    // block descriptors and field layout
+    size_t elems = 0;
+    for (int k = 0; k < bx * by; k++) {
+        const int px = k / by, py = k % by;
+        BlockDesc B{};
+        B.nx = desc->nx_cols[px];
+        B.ny = desc->ny_rows[py];
+        B.pitch = ((B.ny + 2 + kColPad) + 31) / 32 * 32;
+        B.group = 0;
+        B.base = (long long)elems + kColPad;
+        B.dx = desc->dx;
+        B.dy = desc->dy;
+        const int nb[4] = {px > 0 ? k - by : -1, px < bx - 1 ? k + by : -1, py > 0 ? k - 1 : -1,
+                           py < by - 1 ? k + 1 : -1};
+        for (int s = 0; s < 4; s++) {
+            B.nbr[s] = nb[s];
+            B.bnd[s] = nb[s] >= 0 ? CONNECT_WITHIN_RANK : desc->boundary[s];
+        }
+        elems += size_t(B.nx + 2) * size_t(B.pitch);
+        D->maxPerimeter = std::max(D->maxPerimeter, 2 * B.nx + 2 * B.ny + 4);
+        D->blocks.push_back(B);
+    }
+    elems += 32;  // slack so the last column's padding stays inside the allocation
+    D->fieldElems = elems;
+    for (int k = 0; k < int(D->blocks.size()); k++) {
+        const BlockDesc &B = D->blocks[k];
+        for (int y0 = 1; y0 <= B.ny; y0 += D->tileRows)
+            for (int x0 = 1; x0 <= B.nx; x0 += D->tileCols)
+                D->units.push_back(WorkUnit{k, y0, x0, std::min(x0 + D->tileCols, B.nx + 1)});
+    }
+    GroupState g0{};
+    g0.units = int(D->units.size());
+    g0.firstBlock = 0;
+    g0.target = INFINITY;
+    g0.dt = 0.f;
+    D->groupsInit.assign(1, g0);
+    D->ngroups = 1;
+
+    bool ok = true;
+    const size_t bytes = elems * sizeof(float);
+    for (int i = 0; i < 2 && ok; i++)
+        ok = cudaMalloc(&D->h[i], bytes) == cudaSuccess && cudaMalloc(&D->hu[i], bytes) == cudaSuccess &&
+             cudaMalloc(&D->hv[i], bytes) == cudaSuccess;
+    ok = ok && cudaMalloc(&D->b, bytes) == cudaSuccess;
+    ok = ok && cudaMalloc(&D->dBlocks, sizeof(BlockDesc) * D->blocks.size()) == cudaSuccess;
+    ok = ok && cudaMalloc(&D->dUnits, sizeof(WorkUnit) * D->units.size()) == cudaSuccess;
+    ok = ok && cudaMalloc(&D->dGroups, sizeof(GroupState) * D->ngroups) == cudaSuccess;
+    if (!ok) {
+        cudaGetLastError();
+        freeDomain(D);
+        return fail(SWE_GPU_ERR_NOMEM, "device allocation of %.1f MB failed", 7.0 * bytes / 1e6);
+    }
+    for (int i = 0; i < 2; i++) {
+        cudaMemsetAsync(D->h[i], 0, bytes, D->stream);
+        cudaMemsetAsync(D->hu[i], 0, bytes, D->stream);
+        cudaMemsetAsync(D->hv[i], 0, bytes, D->stream);
+    }
+    cudaMemsetAsync(D->b, 0, bytes, D->stream);
+    cudaMemcpyAsync(D->dBlocks, D->blocks.data(), sizeof(BlockDesc) * D->blocks.size(), cudaMemcpyHostToDevice, D->stream);
+    cudaMemcpyAsync(D->dUnits, D->units.data(), sizeof(WorkUnit) * D->units.size(), cudaMemcpyHostToDevice, D->stream);
+    cudaMemcpyAsync(D->dGroups, D->groupsInit.data(), sizeof(GroupState) * D->ngroups, cudaMemcpyHostToDevice, D->stream);
+    e = cudaStreamSynchronize(D->stream);
+    if (e != cudaSuccess) {
+        freeDomain(D);
+        return fail(SWE_GPU_ERR_CUDA, "domain initialisation: %s", cudaGetErrorString(e));
+    }
+    for (int i = 0; i < 2; i++) {
+        D->dev.h[i] = D->h[i];
+        D->dev.hu[i] = D->hu[i];
+        D->dev.hv[i] = D->hv[i];
+    }
+    D->dev.b = D->b;
+    D->dev.blocks = D->dBlocks;
+    D->dev.units = D->dUnits;
+    D->dev.groups = D->dGroups;
+    D->dev.nblocks = int(D->blocks.size());
+    D->dev.solver = D->solver;
+    D->dev.semantics = D->semantics;
+    D->dev.splitDtMode = D->splitDtMode;
+    *out = D;
+    return SWE_GPU_OK;
+}
+
+int swe_gpu_domain_destroy(swe_gpu_domain *dom) {
+    if (!dom) return fail(SWE_GPU_ERR_INVALID, "null domain handle");
+    cudaSetDevice(dom->device);
+    cudaStreamSynchronize(dom->stream);
+    freeDomain(dom);
+    return SWE_GPU_OK;
+}
+
+int swe_gpu_block_count(const swe_gpu_domain *dom, int *count) {
+    if (!dom || !count) return fail(SWE_GPU_ERR_INVALID, "null argument");
+    *count = int(dom->blocks.size());
+    return SWE_GPU_OK;
+}
+
+int swe_gpu_block_shape(const swe_gpu_domain *dom, int block, int *nx, int *ny) {
+    int rc = checkBlock(dom, block);
+    if (rc) return rc;
+    if (nx) *nx = dom->blocks[block].nx;
+    if (ny) *ny = dom->blocks[block].ny;
+    return SWE_GPU_OK;
+}
+
+static int transferBlock(swe_gpu_domain *D, int block, float *h, float *hu, float *hv, float *b, int ld, bool up) {
+    int rc = checkBlock(D, block);
+    if (rc) return rc;
+    const BlockDesc &B = D->blocks[block];
+    if (ld < B.ny + 2) return fail(SWE_GPU_ERR_INVALID, "ld %d < ny+2 = %d", ld, B.ny + 2);
+    CUDA_TRY(cudaSetDevice(D->device));
+    std::vector<GroupState> g;
+    rc = readGroups(D, g);
+    if (rc) return rc;
+    const int cur = g[B.group].cur;
+    float *dev[4] = {D->h[cur] + B.base, D->hu[cur] + B.base, D->hv[cur] + B.base, D->b + B.base};
+    float *host[4] = {h, hu, hv, b};
+    for (int f = 0; f < 4; f++) {
+        if (!host[f]) continue;
+        if (up)
+            CUDA_TRY(cudaMemcpy2DAsync(dev[f], size_t(B.pitch) * 4, host[f], size_t(ld) * 4, size_t(B.ny + 2) * 4,
+                                       size_t(B.nx + 2), cudaMemcpyHostToDevice, D->stream));
+        else
+            CUDA_TRY(cudaMemcpy2DAsync(host[f], size_t(ld) * 4, dev[f], size_t(B.pitch) * 4, size_t(B.ny + 2) * 4,
+                                       size_t(B.nx + 2), cudaMemcpyDeviceToHost, D->stream));
+    }
+    CUDA_TRY(cudaStreamSynchronize(D->stream));
+    return SWE_GPU_OK;
+}
+
+int swe_gpu_upload_block(swe_gpu_domain *dom, int block, const float *h, const float *hu, const float *hv,
+                         const float *b, int ld) {
+    return transferBlock(dom, block, const_cast<float *>(h), const_cast<float *>(hu), const_cast<float *>(hv),
+                         const_cast<float *>(b), ld, true);
+}
+
+int swe_gpu_download_block(swe_gpu_domain *dom, int block, float *h, float *hu, float *hv, float *b, int ld) {
+    return transferBlock(dom, block, h, hu, hv, b, ld, false);
+}
+
+int swe_gpu_exchange_bathymetry(swe_gpu_domain *dom) {
+    if (!dom) return fail(SWE_GPU_ERR_INVALID, "null domain handle");
+    CUDA_TRY(cudaSetDevice(dom->device));
+    return enqueueGhost(dom, 1);
+}
+
+int swe_gpu_set_ghost_layer(swe_gpu_domain *dom) {
+    if (!dom) return fail(SWE_GPU_ERR_INVALID, "null domain handle");
+    CUDA_TRY(cudaSetDevice(dom->device));
+    return enqueueGhost(dom, 0);
+}
+
+int swe_gpu_compute_fluxes(swe_gpu_domain *dom) {
+    if (!dom) return fail(SWE_GPU_ERR_INVALID, "null domain handle");
+    CUDA_TRY(cudaSetDevice(dom->device));
+    return enqueueSpeed(dom);
+}
+
+int swe_gpu_update_unknowns(swe_gpu_domain *dom, float dt) {
+    (void)dt;
+    if (!dom) return fail(SWE_GPU_ERR_INVALID, "null domain handle");
+    CUDA_TRY(cudaSetDevice(dom->device));
+    return enqueueUpdate(dom);
+}
+
+int swe_gpu_get_max_timestep(swe_gpu_domain *dom, float *dt) {
+    if (!dom || !dt) return fail(SWE_GPU_ERR_INVALID, "null argument");
+    CUDA_TRY(cudaSetDevice(dom->device));
+    std::vector<GroupState> g;
+    int rc = readGroups(dom, g);
+    if (rc) return rc;
+    *dt = g[0].dt;
+    return SWE_GPU_OK;
+}
+
+int swe_gpu_step(swe_gpu_domain *dom, int nsteps) {
+    if (!dom || nsteps < 0) return fail(SWE_GPU_ERR_INVALID, "bad argument");
+    CUDA_TRY(cudaSetDevice(dom->device));
+    for (int i = 0; i < nsteps; i++) {
+        int rc = enqueueStep(dom);
+        if (rc) return rc;
+    }
+    return SWE_GPU_OK;
+}
+
+int swe_gpu_advance(swe_gpu_domain *dom, float t_end, int max_steps, int *steps_done, float *t_now) {
+    if (!dom || max_steps < 0) return fail(SWE_GPU_ERR_INVALID, "bad argument");
+    CUDA_TRY(cudaSetDevice(dom->device));
+    const int batch = 16;
+    if (!dom->graph) {  // capture `batch` steps once; replays are identical
+        cudaGraph_t g;
+        CUDA_TRY(cudaStreamBeginCapture(dom->stream, cudaStreamCaptureModeThreadLocal));
+        int rc = SWE_GPU_OK;
+        for (int i = 0; i < batch && rc == SWE_GPU_OK; i++) rc = enqueueStep(dom);
+        cudaError_t e = cudaStreamEndCapture(dom->stream, &g);
+        if (rc) return rc;
+        if (e != cudaSuccess) return fail(SWE_GPU_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&dom->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return fail(SWE_GPU_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+        dom->graphSteps = batch;
+    }
+    std::vector<GroupState> g;
+    int rc = readGroups(dom, g);
+    if (rc) return rc;
+    const int startSteps = g[0].steps;
+    rc = setTargets(dom, t_end);
+    if (rc) return rc;
+    int done = 0;
+    while (done < max_steps) {
+        const int remaining = max_steps - done;
+        if (remaining >= dom->graphSteps) {
+            CUDA_TRY(cudaGraphLaunch(dom->graph, dom->stream));
+        } else {
+            for (int i = 0; i < remaining; i++) {
+                rc = enqueueStep(dom);
+                if (rc) return rc;
+            }
+        }
+        rc = readGroups(dom, g);
+        if (rc) return rc;
+        done = g[0].steps - startSteps;
+        if (!(g[0].time < t_end)) break;
+    }
+    rc = setTargets(dom, INFINITY);
+    if (rc) return rc;
+    if (steps_done) *steps_done = done;
+    if (t_now) *t_now = g[0].time;
+    if (g[0].status) return fail(SWE_GPU_ERR_DEVICE, "device status 0x%x (NaN wave speed)", g[0].status);
+    return SWE_GPU_OK;
+}
+
+int swe_gpu_get_time(swe_gpu_domain *dom, float *t, int *steps) {
+    if (!dom) return fail(SWE_GPU_ERR_INVALID, "null domain handle");
+    CUDA_TRY(cudaSetDevice(dom->device));
+    std::vector<GroupState> g;
+    int rc = readGroups(dom, g);
+    if (rc) return rc;
+    if (t) *t = g[0].time;
+    if (steps) *steps = g[0].steps;
+    return SWE_GPU_OK;
+}
+
+int swe_gpu_set_time(swe_gpu_domain *dom, float t) {
+    if (!dom) return fail(SWE_GPU_ERR_INVALID, "null domain handle");
+    CUDA_TRY(cudaSetDevice(dom->device));
+    for (int gi = 0; gi < dom->ngroups; gi++)
+        CUDA_TRY(cudaMemcpyAsync(&dom->dGroups[gi].time, &t, sizeof(float), cudaMemcpyHostToDevice, dom->stream));
+    CUDA_TRY(cudaStreamSynchronize(dom->stream));
+    return SWE_GPU_OK;
+}
+
+int swe_gpu_sync(swe_gpu_domain *dom) {
+    if (!dom) return fail(SWE_GPU_ERR_INVALID, "null domain handle");
+    CUDA_TRY(cudaSetDevice(dom->device));
+    CUDA_TRY(cudaStreamSynchronize(dom->stream));
+    return SWE_GPU_OK;
+}
+
+int swe_gpu_status(swe_gpu_domain *dom, int *status) {
+    if (!dom || !status) return fail(SWE_GPU_ERR_INVALID, "null argument");
+    CUDA_TRY(cudaSetDevice(dom->device));
+    std::vector<GroupState> g;
+    int rc = readGroups(dom, g);
+    if (rc) return rc;
+    int s = 0;
+    for (auto &x : g) s |= x.status;
+    *status = s;
+    return SWE_GPU_OK;
+}
+
+int swe_gpu_get_stream(swe_gpu_domain *dom, void **stream) {
+    if (!dom || !stream) return fail(SWE_GPU_ERR_INVALID, "null argument");
+    *stream = dom->stream;
+    return SWE_GPU_OK;
+}
+
+int swe_gpu_set_stream(swe_gpu_domain *dom, void *stream) {
+    if (!dom) return fail(SWE_GPU_ERR_INVALID, "null domain handle");
+    CUDA_TRY(cudaSetDevice(dom->device));
+    CUDA_TRY(cudaStreamSynchronize(dom->stream));
+    dom->stream = stream ? static_cast<cudaStream_t>(stream) : dom->ownStream;
+    return SWE_GPU_OK;
+}
+
+int swe_gpu_solve_edges(int solver, long long n, const float *hL, const float *hR, const float *huL,
+                        const float *huR, const float *bL, const float *bR, float *hUpdL, float *hUpdR,
+                        float *huUpdL, float *huUpdR, float *maxWaveSpeed, void *stream) {
+    if (n < 0) return fail(SWE_GPU_ERR_INVALID, "negative edge count");
+    if (n == 0) return SWE_GPU_OK;
+    const int th = 256;
+    const unsigned blocks = unsigned((n + th - 1) / th);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    switch (solver) {
+    case SWE_SOLVER_FWAVE: solveEdgesKernel<SOLVER_FWAVE><<<blocks, th, 0, s>>>(n, hL, hR, huL, huR, bL, bR, hUpdL, hUpdR, huUpdL, huUpdR, maxWaveSpeed); break;
+    case SWE_SOLVER_AUGRIE: solveEdgesKernel<SOLVER_AUGRIE><<<blocks, th, 0, s>>>(n, hL, hR, huL, huR, bL, bR, hUpdL, hUpdR, huUpdL, huUpdR, maxWaveSpeed); break;
+    case SWE_SOLVER_HYBRID: solveEdgesKernel<SOLVER_HYBRID><<<blocks, th, 0, s>>>(n, hL, hR, huL, huR, bL, bR, hUpdL, hUpdR, huUpdL, huUpdR, maxWaveSpeed); break;
+    case SWE_SOLVER_HLLE: solveEdgesKernel<SOLVER_HLLE><<<blocks, th, 0, s>>>(n, hL, hR, huL, huR, bL, bR, hUpdL, hUpdR, huUpdL, huUpdR, maxWaveSpeed); break;
+    default: return fail(SWE_GPU_ERR_INVALID, "unknown solver %d", solver);
+    }
+    CUDA_TRY(cudaGetLastError());
+    return SWE_GPU_OK;
+}
+
+} // extern "C"

@@ -1,0 +1,422 @@
+// Device-side data layout and Riemann solvers of the GB300 block step.
+//
+// Layout (HBM): every block owns (nx+2) columns of `pitch` floats per field,
+// column x at base + x*pitch, element (x, y) at base + x*pitch + y -- the
+// Float2D order of the reference (a[x][y], y contiguous; src/tools/Float2D.hh:74-76)
+// with each column shifted by kColPad floats so the first interior row y = 1
+// starts on a 128-byte boundary (pitch is a multiple of 32 floats).  h, hu, hv
+// are double-buffered (a step reads buffer p and writes buffer p^1, so tiles
+// can read their neighbours' halo without racing the update); b is single.
+//
+// Solvers: the f-wave, HLLE and augmented Riemann solvers restated from the
+// published methods (Bale et al. 2002; Einfeldt 1988; George 2008) with the
+// swe_solvers argument convention of the reference's call sites
+// (src/blocks/SWE_DimensionalSplittingMpi.cpp:403-410).  Every fused
+// multiply-add is an explicit fmaf; the library is compiled with -fmad=false,
+// IEEE division and square root, so results are reproducible bit for bit.
+#pragma once
+
+#include <cfloat>
+#include <cstdint>
+
+namespace swegb {
+
+constexpr float kG = 9.81f;
+constexpr float kHalfG = 0.5f * 9.81f;  // exact in float
+constexpr float kDryTol = 0.01f;        // solver dry tolerance
+constexpr float kZeroTol = 1e-7f;       // |s| below this: wave split evenly
+constexpr int kColPad = 31;             // y = 0 sits at offset 31 of a column
+constexpr int kMaxTileRows = 256;       // threads per CTA (one row each)
+constexpr int kMaxTileCols = 128;       // columns per x-chunk
+
+enum SolverId { SOLVER_FWAVE = 1, SOLVER_AUGRIE = 2, SOLVER_HYBRID = 3, SOLVER_HLLE = 4 };
+enum Semantics { SEM_UNSPLIT = 0, SEM_SPLIT = 1 };
+enum BoundaryType { OUTFLOW = 0, WALL = 1, INFLOW = 2, CONNECT = 3, CONNECT_WITHIN_RANK = 4, PASSIVE = 5 };
+enum SplitDtMode { SPLIT_DT_MAX = 0, SPLIT_DT_LAST_EDGE = 1 };
+
+struct BlockDesc {
+    int nx, ny;       // interior cells
+    int pitch;        // floats per column
+    int group;        // dt group (one per independent simulation)
+    long long base;   // element offset of cell (0, 0)
+    int bnd[4];       // boundary types LEFT, RIGHT, BOTTOM, TOP
+    int nbr[4];       // neighbour block ids (CONNECT_WITHIN_RANK) or -1
+    float dx, dy;
+};
+
+// work unit of the sweep kernels: one block, rows [y0, y0+TY) x columns [x0, x1)
+struct WorkUnit {
+    int block, y0, x0, x1;
+};
+
+// Per dt-group control block, device-resident.  Kernels of a step skip the
+// group once time >= target (so a batch of steps can be queued ahead and stops
+// where the reference's `while (t < checkpoint)` loop stops); the last CTA of
+// each pass (arrival counter) finishes the pass: dt after the speed pass,
+// time/steps/current buffer after the update pass.
+struct GroupState {
+    unsigned int speedBits;  // max wave speed of the running step (float bits)
+    unsigned int arrived;    // CTAs of the running pass that have finished
+    int units;               // CTAs per pass in this group
+    int firstBlock;          // the group's first block (its dx, dy)
+    float dt;                // maxTimestep of the last speed pass
+    float speed;             // max wave speed of the last speed pass
+    float time;              // simulated time (float, like the drivers' t)
+    float target;            // steps run only while time < target
+    int steps;               // executed steps
+    int cur;                 // buffer (0/1) holding the current state
+    int status;              // bit 0: NaN wave speed, bit 1: non-finite water height produced
+    int pad;
+};
+
+struct DomainDev {
+    float *h[2], *hu[2], *hv[2];
+    float *b;
+    const BlockDesc *blocks;
+    const WorkUnit *units;
+    GroupState *groups;
+    int nblocks;
+    int solver, semantics, splitDtMode;
+};
+
+__device__ __forceinline__ float vmin(float a, float b) { return (b < a) ? b : a; }
+__device__ __forceinline__ float vmax(float a, float b) { return (a < b) ? b : a; }
+
+// ---------------------------------------------------------------------------
+// Per-cell quantities shared by the four edges of a cell (f-wave / HLLE):
+// h, normal momentum hn, b, u = hn/h, sqrt(h), sqrt(g h).  Dry cells keep
+// their raw values; their derived values are never used.
+// ---------------------------------------------------------------------------
+struct Cell {
+    float h, hn, b, u, sq, c;
+};
+
+__device__ __forceinline__ Cell makeCell(float h, float hn, float b, float u, float sq, float c) {
+    Cell q;
+    q.h = h; q.hn = hn; q.b = b; q.u = u; q.sq = sq; q.c = c;
+    return q;
+}
+
+__device__ __forceinline__ void routeWave(float s, float zh, float zhu, float &hL, float &hR, float &huL, float &huR) {
+    if (s < -kZeroTol) {
+        hL += zh;
+        huL += zhu;
+    } else if (s > kZeroTol) {
+        hR += zh;
+        huR += zhu;
+    } else {
+        const float a = 0.5f * zh;
+        const float c = 0.5f * zhu;
+        hL += a;
+        huL += c;
+        hR += a;
+        huR += c;
+    }
+}
+
+// wet/dry pre-step of the f-wave and HLLE solvers: a dry side becomes the
+// reflection of the wet side (a wall).  Returns false for a dry/dry edge.
+__device__ __forceinline__ bool reflectDry(Cell &L, Cell &R, bool &dryL, bool &dryR) {
+    dryL = L.h < kDryTol;
+    dryR = R.h < kDryTol;
+    if (dryL && dryR) return false;
+    if (dryL) {
+        L.h = R.h; L.hn = -R.hn; L.u = -R.u; L.sq = R.sq; L.c = R.c; L.b = R.b;
+    } else if (dryR) {
+        R.h = L.h; R.hn = -L.hn; R.u = -L.u; R.sq = L.sq; R.c = L.c; R.b = L.b;
+    }
+    return true;
+}
+
+template <int S>
+__device__ __forceinline__ void waveSpeeds(const Cell &L, const Cell &R, float &s1, float &s2) {
+    const float uRoe = fmaf(L.u, L.sq, R.u * R.sq) / (L.sq + R.sq);
+    const float cRoe = sqrtf(kG * (0.5f * (L.h + R.h)));
+    if (S == SOLVER_FWAVE) {
+        s1 = uRoe - cRoe;
+        s2 = uRoe + cRoe;
+    } else {
+        s1 = vmin(L.u - L.c, uRoe - cRoe);
+        s2 = vmax(R.u + R.c, uRoe + cRoe);
+    }
+}
+
+/// f-wave (S = SOLVER_FWAVE) or HLLE (S = SOLVER_HLLE) net updates of one edge.
+template <int S>
+__device__ __forceinline__ void edgeFH(Cell L, Cell R, float &hUpdL, float &hUpdR, float &huUpdL, float &huUpdR,
+                                       float &speed) {
+    hUpdL = 0.f; hUpdR = 0.f; huUpdL = 0.f; huUpdR = 0.f;
+    bool dryL, dryR;
+    if (!reflectDry(L, R, dryL, dryR)) {
+        speed = 0.f;
+        return;
+    }
+    float s1, s2;
+    waveSpeeds<S>(L, R, s1, s2);
+    const float df1 = R.hn - L.hn;
+    const float phiL = fmaf(L.hn, L.u, kHalfG * L.h * L.h);
+    const float phiR = fmaf(R.hn, R.u, kHalfG * R.h * R.h);
+    const float df2 = (phiR - phiL) + kHalfG * (L.h + R.h) * (R.b - L.b);
+    const float rd = 1.f / (s2 - s1);
+    const float beta1 = fmaf(s2, df1, -df2) * rd;
+    const float beta2 = fmaf(-s1, df1, df2) * rd;
+    routeWave(s1, beta1, beta1 * s1, hUpdL, hUpdR, huUpdL, huUpdR);
+    routeWave(s2, beta2, beta2 * s2, hUpdL, hUpdR, huUpdL, huUpdR);
+    if (dryL) { hUpdL = 0.f; huUpdL = 0.f; }
+    if (dryR) { hUpdR = 0.f; huUpdR = 0.f; }
+    speed = vmax(fabsf(s1), fabsf(s2));
+}
+
+/// max wave speed of one edge, bit-identical to edgeFH's `speed`
+template <int S> __device__ __forceinline__ float edgeSpeedFH(Cell L, Cell R) {
+    bool dryL, dryR;
+    if (!reflectDry(L, R, dryL, dryR)) return 0.f;
+    float s1, s2;
+    waveSpeeds<S>(L, R, s1, s2);
+    return vmax(fabsf(s1), fabsf(s2));
+}
+
+// ---------------------------------------------------------------------------
+// Augmented Riemann solver (George 2008): per-edge, same operation order as
+// the CPU restatement it is tested against.
+// ---------------------------------------------------------------------------
+struct AugRieParams {
+    static constexpr float newtonTol = 1e-6f;
+    static constexpr int maxNewton = 1;
+    static constexpr float critTol = 1e-6f;
+};
+
+__device__ __forceinline__ void waveCurve(float h, float hK, float cK, float &f, float &df) {
+    if (h > hK) {
+        const float s = sqrtf(0.5f * kG * (1.f / h + 1.f / hK));
+        f = (h - hK) * s;
+        df = s - kG * (h - hK) / (4.f * h * h * s);
+    } else {
+        f = 2.f * (sqrtf(kG * h) - cK);
+        df = sqrtf(kG / h);
+    }
+}
+
+static __device__ __noinline__ void middleState(float hL, float hR, float uL, float uR, float &hm, float &s1m, float &s2m,
+                                         bool &rare1, bool &rare2) {
+    if (hR < kDryTol) {
+        hm = 0.f;
+        const float front = uL + 2.f * sqrtf(kG * hL);
+        s1m = front; s2m = front; rare1 = true; rare2 = false;
+        return;
+    }
+    if (hL < kDryTol) {
+        hm = 0.f;
+        const float front = uR - 2.f * sqrtf(kG * hR);
+        s1m = front; s2m = front; rare1 = false; rare2 = true;
+        return;
+    }
+    const float cL = sqrtf(kG * hL);
+    const float cR = sqrtf(kG * hR);
+    const float cm = 0.5f * (cL + cR) + 0.25f * (uL - uR);
+    if (cm <= 0.f) {
+        hm = 0.f;
+        s1m = uL + 2.f * cL; s2m = uR - 2.f * cR; rare1 = true; rare2 = true;
+        return;
+    }
+    const float hRR = cm * cm / kG;
+    float um;
+    if (hRR <= vmin(hL, hR)) {
+        hm = hRR;
+        um = uL + 2.f * (cL - cm);
+        rare1 = true; rare2 = true;
+    } else {
+        float h = hRR;
+        for (int it = 0; it < AugRieParams::maxNewton; ++it) {
+            float fL, dfL, fR, dfR;
+            waveCurve(h, hL, cL, fL, dfL);
+            waveCurve(h, hR, cR, fR, dfR);
+            const float F = fL + fR + (uR - uL);
+            if (fabsf(F) < AugRieParams::newtonTol) break;
+            h = h - F / (dfL + dfR);
+            if (h < kDryTol) {
+                h = kDryTol;
+                break;
+            }
+        }
+        hm = h;
+        float fL, dfL;
+        waveCurve(hm, hL, cL, fL, dfL);
+        um = uL - fL;
+        rare1 = hm <= hL;
+        rare2 = hm <= hR;
+    }
+    const float cmid = sqrtf(kG * hm);
+    s1m = um - cmid;
+    s2m = um + cmid;
+}
+
+static __device__ __noinline__ void edgeAugRie(float hL, float hR, float huL, float huR, float bL, float bR, float &hUpdL,
+                                        float &hUpdR, float &huUpdL, float &huUpdR, float &speed) {
+    const bool dryL = hL < kDryTol;
+    const bool dryR = hR < kDryTol;
+    hUpdL = 0.f; hUpdR = 0.f; huUpdL = 0.f; huUpdR = 0.f;
+    if (dryL && dryR) {
+        speed = 0.f;
+        return;
+    }
+    float uL = 0.f, uR = 0.f;
+    bool wallL = false, wallR = false;
+    if (dryR) {
+        uL = huL / hL;
+        float hm, s1m, s2m;
+        bool r1, r2;
+        middleState(hL, hL, uL, -uL, hm, s1m, s2m, r1, r2);
+        const float hTest = vmax(hL, hm);
+        if (hTest + bL < bR) {
+            wallR = true;
+            hR = hL; huR = -huL; uR = -uL; bR = bL;
+        } else {
+            hR = 0.f; huR = 0.f;
+        }
+    } else if (dryL) {
+        uR = huR / hR;
+        float hm, s1m, s2m;
+        bool r1, r2;
+        middleState(hR, hR, -uR, uR, hm, s1m, s2m, r1, r2);
+        const float hTest = vmax(hR, hm);
+        if (hTest + bR < bL) {
+            wallL = true;
+            hL = hR; huL = -huR; uL = -uR; bL = bR;
+        } else {
+            hL = 0.f; huL = 0.f;
+        }
+    } else {
+        uL = huL / hL;
+        uR = huR / hR;
+    }
+
+    float hm, s1m, s2m;
+    bool rare1, rare2;
+    middleState(hL, hR, uL, uR, hm, s1m, s2m, rare1, rare2);
+
+    const float cL = sqrtf(kG * hL);
+    const float cR = sqrtf(kG * hR);
+    const float sqL = sqrtf(hL);
+    const float sqR = sqrtf(hR);
+    const float uRoe = fmaf(uL, sqL, uR * sqR) / (sqL + sqR);
+    const float cRoe = sqrtf(kG * (0.5f * (hL + hR)));
+    const float sE1 = vmin(uL - cL, uRoe - cRoe);
+    const float sE2 = vmax(uR + cR, uRoe + cRoe);
+    const float l1 = vmin(sE1, s1m);
+    const float l3 = vmax(sE2, s2m);
+
+    const float hStarHLL = vmax((huL - huR + l3 * hR - l1 * hL) / (l3 - l1), 0.f);
+
+    float l2 = 0.5f * (l1 + l3);
+    bool corrector = false;
+    if (rare1 && l1 < 0.f && s1m > 0.f) {
+        l2 = s1m;
+        corrector = true;
+    } else if (rare2 && s2m < 0.f && l3 > 0.f) {
+        l2 = s2m;
+        corrector = true;
+    }
+    if (corrector && !(l1 < l2 && l2 < l3)) corrector = false;
+    if (corrector && vmin(hL, hR) < kDryTol) corrector = false;
+    if (!corrector) l2 = 0.5f * (l1 + l3);
+
+    const float dh = hR - hL;
+    const float dhu = huR - huL;
+    const float phiL = fmaf(huL, uL, kHalfG * hL * hL);
+    const float phiR = fmaf(huR, uR, kHalfG * hR * hR);
+    const float dphi = phiR - phiL;
+    const float db = bR - bL;
+
+    const float critTol = AugRieParams::critTol;
+    const float hbar = vmax(0.5f * (hL + hR), 0.f);
+    const float uSum = uL + uR;
+    const float s1s2bar = 0.25f * uSum * uSum - kG * hbar;
+    const float s1s2tilde = vmax(0.f, uL * uR) - kG * hbar;
+
+    bool sonic = false;
+    if (fabsf(s1s2bar) <= critTol) sonic = true;
+    if (s1s2bar * s1s2tilde <= critTol) sonic = true;
+    if (s1s2bar * l1 * l3 <= critTol) sonic = true;
+    if (vmin(fabsf(l1), fabsf(l3)) < critTol) sonic = true;
+    if (l1 < 0.f && s1m > 0.f) sonic = true;
+    if (l3 > 0.f && s2m < 0.f) sonic = true;
+    if ((uL + cL) * (uR + cR) < 0.f) sonic = true;
+    if ((uL - cL) * (uR - cR) < 0.f) sonic = true;
+
+    float ddh = sonic ? -db : db * kG * hbar / s1s2bar;
+    const float width = l3 - l1;
+    if (l1 < -critTol && l3 > critTol) {
+        ddh = vmin(ddh, hStarHLL * width / l3);
+        ddh = vmax(ddh, hStarHLL * width / l1);
+    } else if (l1 >= critTol) {
+        ddh = vmin(ddh, hStarHLL * width / l1);
+        ddh = vmax(ddh, -hL);
+    } else if (l3 <= -critTol) {
+        ddh = vmin(ddh, hR);
+        ddh = vmax(ddh, hStarHLL * width / l3);
+    }
+    float ddphi = sonic ? -kG * hbar * db : -db * kG * hbar * s1s2tilde / s1s2bar;
+    const float pL = -hL * db;
+    const float pR = -hR * db;
+    ddphi = vmin(ddphi, kG * vmax(pL, pR));
+    ddphi = vmax(ddphi, kG * vmin(pL, pR));
+
+    const float d1 = dh - ddh;
+    const float d2 = dhu;
+    const float d3 = dphi - ddphi;
+
+    float beta1, beta2, beta3;
+    if (!corrector) {
+        const float rd = 1.f / width;
+        beta1 = fmaf(l3, d1, -d2) * rd;
+        beta3 = fmaf(-l1, d1, d2) * rd;
+        beta2 = d3 - l1 * (l1 * beta1) - l3 * (l3 * beta3);
+    } else {
+        beta1 = (l2 * l3 * d1 - (l2 + l3) * d2 + d3) / ((l1 - l2) * (l1 - l3));
+        beta2 = (l1 * l3 * d1 - (l1 + l3) * d2 + d3) / ((l2 - l1) * (l2 - l3));
+        beta3 = (l1 * l2 * d1 - (l1 + l2) * d2 + d3) / ((l3 - l1) * (l3 - l2));
+    }
+    routeWave(l1, beta1 * l1, beta1 * l1 * l1, hUpdL, hUpdR, huUpdL, huUpdR);
+    if (corrector)
+        routeWave(l2, beta2 * l2, beta2 * l2 * l2, hUpdL, hUpdR, huUpdL, huUpdR);
+    else
+        routeWave(l2, 0.f, beta2, hUpdL, hUpdR, huUpdL, huUpdR);
+    routeWave(l3, beta3 * l3, beta3 * l3 * l3, hUpdL, hUpdR, huUpdL, huUpdR);
+
+    if (wallL) { hUpdL = 0.f; huUpdL = 0.f; }
+    if (wallR) { hUpdR = 0.f; huUpdR = 0.f; }
+    speed = vmax(fabsf(l1), fabsf(l3));
+}
+
+/// the switch of the hybrid solver: augmented solver where either side is
+/// shallower than 0.1 m, f-wave elsewhere
+constexpr float kHybridSwitchDepth = 0.1f;
+
+/// Full edge solve for any solver from per-cell quantities.
+template <int S>
+__device__ __forceinline__ void edgeSolve(const Cell &L, const Cell &R, float &hUpdL, float &hUpdR, float &huUpdL,
+                                          float &huUpdR, float &speed) {
+    if (S == SOLVER_FWAVE || S == SOLVER_HLLE) {
+        edgeFH<S>(L, R, hUpdL, hUpdR, huUpdL, huUpdR, speed);
+    } else if (S == SOLVER_AUGRIE) {
+        edgeAugRie(L.h, R.h, L.hn, R.hn, L.b, R.b, hUpdL, hUpdR, huUpdL, huUpdR, speed);
+    } else {
+        if (L.h < kHybridSwitchDepth || R.h < kHybridSwitchDepth)
+            edgeAugRie(L.h, R.h, L.hn, R.hn, L.b, R.b, hUpdL, hUpdR, huUpdL, huUpdR, speed);
+        else
+            edgeFH<SOLVER_FWAVE>(L, R, hUpdL, hUpdR, huUpdL, huUpdR, speed);
+    }
+}
+
+template <int S> __device__ __forceinline__ float edgeSpeed(const Cell &L, const Cell &R) {
+    if (S == SOLVER_FWAVE || S == SOLVER_HLLE) {
+        return edgeSpeedFH<S>(L, R);
+    } else {
+        float a, b, c, d, s;
+        edgeSolve<S>(L, R, a, b, c, d, s);
+        return s;
+    }
+}
+
+} // namespace swegb

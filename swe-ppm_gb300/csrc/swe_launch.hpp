@@ -1,0 +1,28 @@
+// Host-side launchers of the templated step kernels (one translation unit per
+// solver family so the library compiles in parallel).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "swe_device.cuh"
+
+namespace swegb {
+
+// speed pass (computeNumericalFluxes' wave speeds + maxTimestep) and fused
+// solve-and-update pass (updateUnknowns) of the f-wave and HLLE solvers
+cudaError_t launchSpeedFH(const DomainDev &d, int nunits, int threads, cudaStream_t s);
+cudaError_t launchUpdateFH(const DomainDev &d, int nunits, int threads, cudaStream_t s);
+// same for the augmented and hybrid solvers
+cudaError_t launchSpeedAug(const DomainDev &d, int nunits, int threads, cudaStream_t s);
+cudaError_t launchUpdateAug(const DomainDev &d, int nunits, int threads, cudaStream_t s);
+
+inline cudaError_t launchSpeed(const DomainDev &d, int nunits, int threads, cudaStream_t s) {
+    return (d.solver == SOLVER_FWAVE || d.solver == SOLVER_HLLE) ? launchSpeedFH(d, nunits, threads, s)
+                                                                 : launchSpeedAug(d, nunits, threads, s);
+}
+inline cudaError_t launchUpdate(const DomainDev &d, int nunits, int threads, cudaStream_t s) {
+    return (d.solver == SOLVER_FWAVE || d.solver == SOLVER_HLLE) ? launchUpdateFH(d, nunits, threads, s)
+                                                                 : launchUpdateAug(d, nunits, threads, s);
+}
+
+} // namespace swegb

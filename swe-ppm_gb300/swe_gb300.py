@@ -1,0 +1,297 @@
+"""Python binding (ctypes) of the GB300 block step: the C ABI of
+include/swe_gb300.h (device path) and include/swe_gb300_host.h (host set-up).
+
+There is no CPU fallback: every device call goes to the in-tree CUDA library
+(_build/libswe_gb300.so) and raises SweGpuError when the library, the GPU or
+a CUDA call fails.
+
+Block state travels as float32 numpy arrays in the reference's Float2D layout
+(a[x][y] = raw[x*(ny+2)+y], src/tools/Float2D.hh:74-76); for a multi-block
+domain the arrays of all blocks are concatenated in rank order (block k at
+(k // blocks_y, k % blocks_y), src/examples/swe_mpi.cpp:186-187).
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libswe_gb300.so")
+
+FWAVE, AUGRIE, HYBRID, HLLE = 1, 2, 3, 4
+SOLVERS = {"fwave": FWAVE, "augrie": AUGRIE, "hybrid": HYBRID, "hlle": HLLE}
+UNSPLIT, SPLIT = 0, 1
+SPLIT_DT_MAX, SPLIT_DT_LAST_EDGE = 0, 1
+OUTFLOW, WALL, INFLOW, CONNECT, CONNECT_WITHIN_RANK, PASSIVE = range(6)
+
+SCENARIO_RADIAL_DAM_BREAK = 0
+SCENARIO_RADIAL_BATHYMETRY_DAM_BREAK = 1
+SCENARIO_SEA_AT_REST = 2
+SCENARIO_HALF_DOMAIN_DRY = 3
+SCENARIO_BATHYMETRY_DAM_BREAK = 4
+SCENARIO_SPLASHING_POOL = 5
+SCENARIO_SPLASHING_CONE = 6
+SCENARIO_DAM_BREAK = 10
+SCENARIO_TSUNAMI = 11
+SCENARIO_SHORELINE = 12
+
+EXPORTED = [
+    "swe_gpu_domain_create", "swe_gpu_domain_destroy", "swe_gpu_block_count", "swe_gpu_block_shape",
+    "swe_gpu_upload_block", "swe_gpu_download_block", "swe_gpu_exchange_bathymetry", "swe_gpu_set_ghost_layer",
+    "swe_gpu_compute_fluxes", "swe_gpu_update_unknowns", "swe_gpu_get_max_timestep", "swe_gpu_step",
+    "swe_gpu_advance", "swe_gpu_get_time", "swe_gpu_set_time", "swe_gpu_sync", "swe_gpu_status",
+    "swe_gpu_get_stream", "swe_gpu_set_stream", "swe_gpu_last_error", "swe_gpu_version", "swe_gpu_solve_edges",
+    "swe_host_scenario_geometry", "swe_host_scenario_boundary", "swe_host_init_block", "swe_host_decompose",
+]
+
+
+class SweGpuError(RuntimeError):
+    pass
+
+
+class Desc(C.Structure):
+    _fields_ = [("blocks_x", C.c_int), ("blocks_y", C.c_int), ("nx_cols", C.POINTER(C.c_int)),
+                ("ny_rows", C.POINTER(C.c_int)), ("dx", C.c_float), ("dy", C.c_float),
+                ("boundary", C.c_int * 4), ("solver", C.c_int), ("semantics", C.c_int),
+                ("split_dt_mode", C.c_int), ("tile_rows", C.c_int), ("tile_cols", C.c_int), ("device", C.c_int)]
+
+
+_lib = None
+
+
+def build(verbose=False):
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("swe_gb300_build", os.path.join(HERE, "build.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.build(verbose=verbose)
+
+
+def lib():
+    """The in-tree CUDA library; raises when it is missing (no fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise SweGpuError("CUDA library %s is missing: run __graft_entry__.build()" % LIB_PATH)
+        L = C.CDLL(LIB_PATH)
+        vp = C.c_void_p
+        L.swe_gpu_last_error.restype = C.c_char_p
+        L.swe_gpu_domain_create.argtypes = [C.POINTER(Desc), C.POINTER(vp)]
+        L.swe_gpu_domain_destroy.argtypes = [vp]
+        L.swe_gpu_block_count.argtypes = [vp, C.POINTER(C.c_int)]
+        L.swe_gpu_block_shape.argtypes = [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        L.swe_gpu_upload_block.argtypes = [vp, C.c_int, vp, vp, vp, vp, C.c_int]
+        L.swe_gpu_download_block.argtypes = [vp, C.c_int, vp, vp, vp, vp, C.c_int]
+        for n in ("swe_gpu_exchange_bathymetry", "swe_gpu_set_ghost_layer", "swe_gpu_compute_fluxes", "swe_gpu_sync"):
+            getattr(L, n).argtypes = [vp]
+        L.swe_gpu_update_unknowns.argtypes = [vp, C.c_float]
+        L.swe_gpu_get_max_timestep.argtypes = [vp, C.POINTER(C.c_float)]
+        L.swe_gpu_step.argtypes = [vp, C.c_int]
+        L.swe_gpu_advance.argtypes = [vp, C.c_float, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_float)]
+        L.swe_gpu_get_time.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_int)]
+        L.swe_gpu_set_time.argtypes = [vp, C.c_float]
+        L.swe_gpu_status.argtypes = [vp, C.POINTER(C.c_int)]
+        L.swe_gpu_get_stream.argtypes = [vp, C.POINTER(vp)]
+        L.swe_gpu_set_stream.argtypes = [vp, vp]
+        L.swe_gpu_solve_edges.argtypes = [C.c_int, C.c_longlong] + [vp] * 11 + [vp]
+        L.swe_host_scenario_geometry.argtypes = [C.c_int, vp, C.c_int, C.c_int, vp]
+        L.swe_host_scenario_boundary.argtypes = [C.c_int, vp, vp]
+        L.swe_host_init_block.argtypes = [C.c_int, vp, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float,
+                                          C.c_float, vp, vp, vp, vp, vp, C.c_int]
+        L.swe_host_decompose.argtypes = [C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float,
+                                         vp, vp, vp, vp, vp, vp]
+        _lib = L
+    return _lib
+
+
+def _check(rc):
+    if rc != 0:
+        raise SweGpuError("swe_gpu error %d: %s" % (rc, lib().swe_gpu_last_error().decode()))
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _params(params):
+    return np.asarray(list(params or []) + [0.0] * 8, dtype=np.float64)[:8]
+
+
+# ---------------------------------------------------------------------------
+# host-side set-up (initScenario, geometry, decomposition)
+# ---------------------------------------------------------------------------
+def scenario_geometry(scenario, nx, ny, params=None):
+    out = np.empty(4, dtype=np.float32)
+    p = _params(params)
+    if lib().swe_host_scenario_geometry(int(scenario), _p(p), int(nx), int(ny), _p(out)) != 0:
+        raise SweGpuError("unknown scenario %r" % scenario)
+    return tuple(float(v) for v in out)
+
+
+def scenario_boundary(scenario, params=None):
+    out = np.empty(4, dtype=np.int32)
+    p = _params(params)
+    if lib().swe_host_scenario_boundary(int(scenario), _p(p), _p(out)) != 0:
+        raise SweGpuError("unknown scenario %r" % scenario)
+    return [int(v) for v in out]
+
+
+def init_block(scenario, nx, ny, dx, dy, origin_x, origin_y, bnd, params=None):
+    arrs = [np.empty((nx + 2) * (ny + 2), dtype=np.float32) for _ in range(4)]
+    b4 = np.asarray(bnd, dtype=np.int32)
+    p = _params(params)
+    rc = lib().swe_host_init_block(int(scenario), _p(p), nx, ny, dx, dy, origin_x, origin_y, _p(b4),
+                                   *[_p(a) for a in arrs], ny + 2)
+    if rc != 0:
+        raise SweGpuError("init_block failed")
+    return tuple(arrs)
+
+
+def decompose(nx, ny, nblocks, dx, dy, origin_x=0.0, origin_y=0.0):
+    bx, by = C.c_int(), C.c_int()
+    cols = np.empty(nblocks, dtype=np.int32)
+    rows = np.empty(nblocks, dtype=np.int32)
+    ox = np.empty(nblocks, dtype=np.float32)
+    oy = np.empty(nblocks, dtype=np.float32)
+    rc = lib().swe_host_decompose(nx, ny, nblocks, dx, dy, origin_x, origin_y, C.byref(bx), C.byref(by), _p(cols),
+                                  _p(rows), _p(ox), _p(oy))
+    if rc != 0:
+        raise SweGpuError("decompose failed")
+    return (list(cols[:bx.value]), list(rows[:by.value]), list(ox[:bx.value]), list(oy[:by.value]))
+
+
+def init_domain(scenario, nx, ny, nblocks=1, params=None, boundary=None):
+    """The drivers' set-up: geometry, decomposition, per-block initScenario
+    (neighbour sides CONNECT_WITHIN_RANK).  Returns (geometry dict, h, hu, hv, b)."""
+    dx, dy, ox0, oy0 = scenario_geometry(scenario, nx, ny, params)
+    outer = boundary if boundary is not None else scenario_boundary(scenario, params)
+    cols, rows, oxs, oys = decompose(nx, ny, nblocks, dx, dy, ox0, oy0)
+    bx, by = len(cols), len(rows)
+    parts = [[], [], [], []]
+    for k in range(bx * by):
+        px, py = k // by, k % by
+        bnd = [CONNECT_WITHIN_RANK if px > 0 else outer[0], CONNECT_WITHIN_RANK if px < bx - 1 else outer[1],
+               CONNECT_WITHIN_RANK if py > 0 else outer[2], CONNECT_WITHIN_RANK if py < by - 1 else outer[3]]
+        arrs = init_block(scenario, cols[px], rows[py], dx, dy, oxs[px], oys[py], bnd, params)
+        for i in range(4):
+            parts[i].append(arrs[i])
+    geo = dict(dx=dx, dy=dy, nx_cols=cols, ny_rows=rows, boundary=list(outer), origin_x=oxs, origin_y=oys)
+    return (geo,) + tuple(np.concatenate(p) for p in parts)
+
+
+# ---------------------------------------------------------------------------
+# device domain
+# ---------------------------------------------------------------------------
+class Domain:
+    """Blocks of one simulation on the GPU (global time step)."""
+
+    def __init__(self, nx_cols, ny_rows, dx, dy, boundary=(OUTFLOW,) * 4, solver=HLLE, semantics=UNSPLIT,
+                 split_dt_mode=SPLIT_DT_MAX, tile_rows=0, tile_cols=0, device=0):
+        self.nx_cols = [int(v) for v in nx_cols]
+        self.ny_rows = [int(v) for v in ny_rows]
+        self.bx, self.by = len(self.nx_cols), len(self.ny_rows)
+        self._cols = (C.c_int * self.bx)(*self.nx_cols)
+        self._rows = (C.c_int * self.by)(*self.ny_rows)
+        d = Desc()
+        d.blocks_x, d.blocks_y = self.bx, self.by
+        d.nx_cols = C.cast(self._cols, C.POINTER(C.c_int))
+        d.ny_rows = C.cast(self._rows, C.POINTER(C.c_int))
+        d.dx, d.dy = float(dx), float(dy)
+        for i in range(4):
+            d.boundary[i] = int(boundary[i])
+        d.solver, d.semantics, d.split_dt_mode = int(solver), int(semantics), int(split_dt_mode)
+        d.tile_rows, d.tile_cols, d.device = int(tile_rows), int(tile_cols), int(device)
+        self.handle = C.c_void_p()
+        _check(lib().swe_gpu_domain_create(C.byref(d), C.byref(self.handle)))
+        self.shapes = [(self.nx_cols[k // self.by], self.ny_rows[k % self.by]) for k in range(self.bx * self.by)]
+        self.offsets = np.cumsum([0] + [(nx + 2) * (ny + 2) for nx, ny in self.shapes])
+        self.ncells = int(self.offsets[-1])
+
+    def close(self):
+        if getattr(self, "handle", None) and self.handle.value:
+            lib().swe_gpu_domain_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload(self, h=None, hu=None, hv=None, b=None):
+        arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float32).ravel() for a in (h, hu, hv, b)]
+        for k, (nx, ny) in enumerate(self.shapes):
+            o0, o1 = self.offsets[k], self.offsets[k + 1]
+            sl = [None if a is None else a[o0:o1] for a in arrs]
+            _check(lib().swe_gpu_upload_block(self.handle, k, *[_p(a) for a in sl], ny + 2))
+
+    def download(self):
+        arrs = [np.empty(self.ncells, dtype=np.float32) for _ in range(4)]
+        for k, (nx, ny) in enumerate(self.shapes):
+            o0, o1 = self.offsets[k], self.offsets[k + 1]
+            _check(lib().swe_gpu_download_block(self.handle, k, *[_p(a[o0:o1]) for a in arrs], ny + 2))
+        return tuple(arrs)
+
+    def download_into(self, arrs):
+        """download h, hu, hv (and b if a 4th array is given) into preallocated float32 arrays"""
+        arrs = list(arrs) + [None] * (4 - len(arrs))
+        for k, (nx, ny) in enumerate(self.shapes):
+            o0, o1 = self.offsets[k], self.offsets[k + 1]
+            _check(lib().swe_gpu_download_block(self.handle, k, *[None if a is None else _p(a[o0:o1]) for a in arrs],
+                                                ny + 2))
+
+    def exchange_bathymetry(self):
+        _check(lib().swe_gpu_exchange_bathymetry(self.handle))
+
+    def set_ghost_layer(self):
+        _check(lib().swe_gpu_set_ghost_layer(self.handle))
+
+    def compute_fluxes(self):
+        _check(lib().swe_gpu_compute_fluxes(self.handle))
+
+    def update_unknowns(self, dt=0.0):
+        _check(lib().swe_gpu_update_unknowns(self.handle, float(dt)))
+
+    def max_timestep(self):
+        v = C.c_float()
+        _check(lib().swe_gpu_get_max_timestep(self.handle, C.byref(v)))
+        return v.value
+
+    def step(self, n=1):
+        _check(lib().swe_gpu_step(self.handle, int(n)))
+
+    def advance(self, t_end, max_steps=1 << 30):
+        n, t = C.c_int(), C.c_float()
+        _check(lib().swe_gpu_advance(self.handle, float(t_end), int(max_steps), C.byref(n), C.byref(t)))
+        return n.value, t.value
+
+    def time(self):
+        t, n = C.c_float(), C.c_int()
+        _check(lib().swe_gpu_get_time(self.handle, C.byref(t), C.byref(n)))
+        return t.value, n.value
+
+    def set_time(self, t):
+        _check(lib().swe_gpu_set_time(self.handle, float(t)))
+
+    def sync(self):
+        _check(lib().swe_gpu_sync(self.handle))
+
+    def status(self):
+        s = C.c_int()
+        _check(lib().swe_gpu_status(self.handle, C.byref(s)))
+        return s.value
+
+    def stream(self):
+        s = C.c_void_p()
+        _check(lib().swe_gpu_get_stream(self.handle, C.byref(s)))
+        return s.value
+
+    def set_stream(self, stream):
+        """launch on an external cudaStream_t (int handle); None = own stream"""
+        _check(lib().swe_gpu_set_stream(self.handle, C.c_void_p(stream or 0)))
+
+
+def solve_edges_device(solver, ptrs_in, ptrs_out, n, stream=None):
+    """Per-edge solver on device pointers (6 inputs, 5 outputs)."""
+    _check(lib().swe_gpu_solve_edges(int(solver), int(n), *[C.c_void_p(p) for p in ptrs_in],
+                                     *[C.c_void_p(p) for p in ptrs_out], C.c_void_p(stream or 0)))
