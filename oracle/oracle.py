@@ -173,8 +173,8 @@ def ref_lib(macro):
     """Harness compiled with WAVE_PROPAGATION_SOLVER=macro (0 HLLEFun, 1 FWave, 2 AugRie)."""
     if macro not in _ref_libs:
         path = os.path.join(REF_DIR, "libswe_ref_s%d.so" % macro)
-        if not os.path.exists(path):
-            build_reference()
+        if not _ref_libs:
+            build_reference()  # make: rebuilds only what the solver headers or harness changed
         L = C.CDLL(path)
         L.ref_init_block.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float,
                                      C.c_float, C.c_void_p] + [C.c_void_p] * 4

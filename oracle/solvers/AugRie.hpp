@@ -262,9 +262,12 @@ public:
                 }
             }
             hm = h;
-            T fL, dfL;
+            // middle velocity seen from both sides, averaged (equal once the
+            // iteration has converged; keeps the estimate mirror-symmetric)
+            T fL, dfL, fR, dfR;
             waveCurve(hm, hL, cL, fL, dfL);
-            um = uL - fL;
+            waveCurve(hm, hR, cR, fR, dfR);
+            um = T(0.5) * ((uL - fL) + (uR + fR));
             rare1 = hm <= hL;
             rare2 = hm <= hR;
         }

@@ -240,9 +240,10 @@ static __device__ __noinline__ void middleState(float hL, float hR, float uL, fl
             }
         }
         hm = h;
-        float fL, dfL;
+        float fL, dfL, fR, dfR;
         waveCurve(hm, hL, cL, fL, dfL);
-        um = uL - fL;
+        waveCurve(hm, hR, cR, fR, dfR);
+        um = 0.5f * ((uL - fL) + (uR + fR));
         rare1 = hm <= hL;
         rare2 = hm <= hR;
     }
