@@ -119,9 +119,8 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def setup_domain(swe, device):
-    geo, h, hu, hv, b = swe.init_domain(swe.SCENARIO_TSUNAMI, N_CELLS_SIDE, N_CELLS_SIDE, N_BLOCKS,
-                                        [N_CELLS_SIDE, SEED, 100000.0])
+def setup_domain(swe, device, n=N_CELLS_SIDE):
+    geo, h, hu, hv, b = swe.init_domain(swe.SCENARIO_TSUNAMI, n, n, N_BLOCKS, [n, SEED, 100000.0])
     tile_rows = int(os.environ.get("SWE_TILE_ROWS", "0"))
     tile_cols = int(os.environ.get("SWE_TILE_COLS", "0"))
     D = swe.Domain(geo["nx_cols"], geo["ny_rows"], geo["dx"], geo["dy"], boundary=geo["boundary"], solver=swe.HLLE,
@@ -185,22 +184,39 @@ def dist_barrier(world):
 
 
 def run_reference(args, world, rank):
+    """The reference's algorithm on the host cores: the oracle (a line-by-line
+    restatement of the reference's block code, bit-identical to it where the
+    reference compiles) with one OpenMP thread per block, like the
+    overdecomposed driver.  One step = one full time step of the 2048^2 domain."""
     if rank != 0:
         return 0
-    steps = []
-    base = None
-    for i in range(args.warmup + args.steps):
-        b = cpu_baseline(seconds=float(os.environ.get("SWE_REF_SECONDS", "8")))
-        if i >= args.warmup:
-            steps.append(b["value"])
-        base = b
-    value = statistics.median(steps)
+    import oracle
+    import swe_gb300 as swe
+    oracle.build()
+    geo, h, hu, hv, b = swe.init_domain(swe.SCENARIO_TSUNAMI, N_CELLS_SIDE, N_CELLS_SIDE, N_BLOCKS,
+                                        [N_CELLS_SIDE, SEED, 100000.0])
+    R = oracle.Domain(geo["nx_cols"], geo["ny_rows"], geo["dx"], geo["dy"], outer=geo["boundary"], solver=oracle.HLLE)
+    R.set_state(h, hu, hv, b)
+    R.bathymetry_ghosts()
+    threads = 1
+    for _ in range(max(args.warmup, 3)):
+        _, threads = R.step_parallel(1)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        R.step_parallel(1)
+        times.append(time.perf_counter() - t0)
+    cells = N_CELLS_SIDE * N_CELLS_SIDE
+    per = sum(times) / len(times)
+    value = cells / per
+    sample = "%d full time steps of the 2048^2 workload, oracle with OpenMP over 16 blocks on %d threads" % (
+        args.steps, threads)
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * base["seconds_per_step"],
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded tsunami scenario)", "config": workload_config({"parallelism": "host cores"}),
-            "cpu_baseline": {"value": value, "unit": "cell-updates/s", "cores": base["cores"], "kind": base["kind"],
-                             "sample": base["sample"]},
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * per, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded tsunami scenario)",
+            "config": workload_config({"parallelism": "host cores"}),
+            "cpu_baseline": {"value": value, "unit": "cell-updates/s", "cores": int(threads), "kind": "port",
+                             "sample": sample},
             "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -211,69 +227,79 @@ def run_gb300(args, world, rank, local):
     import swe_gb300 as swe
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    D, geo, host = setup_domain(swe, local)
-    stream = torch.cuda.current_stream(dev)
+    n = args.cells
+    D, geo, host = setup_domain(swe, local, n)
+    stream = torch.cuda.Stream(dev)  # a real stream handle: the library launches on it
+    assert stream.cuda_stream != 0
     D.set_stream(stream.cuda_stream)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
-    cells = N_CELLS_SIDE * N_CELLS_SIDE
+    cells = n * n
 
-    def one_step():
-        D.set_ghost_layer()
-        D.compute_fluxes()
-        D.update_unknowns()
+    with torch.cuda.stream(stream), ClockSampler(local) as clk:
+        # warm-up: W steps, and at least ~1.5 s of the same load so the clock
+        # samples (taken every 200 ms) describe the timed kernels
+        t_end = time.perf_counter() + (0.0 if args.profile else 1.5)
+        i = 0
+        while i < max(args.warmup, 3) or time.perf_counter() < t_end:
+            flush.zero_()
+            D.step(1)
+            i += 1
+            if i % 64 == 0:
+                stream.synchronize()
+        stream.synchronize()
+        dist_barrier(world)
 
-    for _ in range(max(args.warmup, 3)):
-        flush.zero_()
-        one_step()
-    torch.cuda.synchronize(dev)
-    dist_barrier(world)
-
-    # timed region: K steps, L2 flushed before each, CUDA events around each step
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    with ClockSampler(local) as clk:
-        torch.cuda.synchronize(dev)
+        # timed region: exactly K steps, L2 flushed before each, CUDA events
+        # around each step on the library's stream
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        stream.synchronize()
         dist_barrier(world)
         for i in range(args.steps):
             flush.zero_()
             starts[i].record(stream)
-            one_step()
+            D.step(1)
             ends[i].record(stream)
-        torch.cuda.synchronize(dev)
+        stream.synchronize()
         dist_barrier(world)
-    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    step_ms = [s_.elapsed_time(e) for s_, e in zip(starts, ends)]
     total_ms = dist_max(sum(step_ms), world)
     ms_per_step = total_ms / args.steps
+    if args.profile:
+        if rank == 0:
+            print(json.dumps({"profile_run": True, "cells": cells, "ms_per_step": ms_per_step}), flush=True)
+        D.close()
+        return 0
 
-    # per-kernel breakdown (same region shape, events between the three launches)
+    # per-kernel breakdown: events between the three launches of each step
     ev = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
-    for i in range(args.steps):
-        flush.zero_()
-        ev[i][0].record(stream)
-        D.set_ghost_layer()
-        ev[i][1].record(stream)
-        D.compute_fluxes()
-        ev[i][2].record(stream)
-        D.update_unknowns()
-        ev[i][3].record(stream)
-    torch.cuda.synchronize(dev)
+    with torch.cuda.stream(stream):
+        for i in range(args.steps):
+            flush.zero_()
+            ev[i][0].record(stream)
+            D.set_ghost_layer()
+            ev[i][1].record(stream)
+            D.compute_fluxes()
+            ev[i][2].record(stream)
+            D.update_unknowns()
+            ev[i][3].record(stream)
+        stream.synchronize()
     t_ghost = statistics.mean(e[0].elapsed_time(e[1]) for e in ev)
     t_speed = statistics.mean(e[1].elapsed_time(e[2]) for e in ev)
     t_update = statistics.mean(e[2].elapsed_time(e[3]) for e in ev)
     status = D.status()
 
-    # end to end through the C ABI on host buffers (pinned)
+    # end to end through the C ABI on host buffers: upload h, hu, hv, b from
+    # pinned memory, one step, download h, hu, hv; host clock around it all
     pinned = [torch.from_numpy(a).pin_memory() for a in host]
     outs = [torch.empty(host[0].shape, dtype=torch.float32).pin_memory() for _ in range(3)]
     pn = [p.numpy() for p in pinned]
     on = [o.numpy() for o in outs]
-    e2e_steps = max(3, min(args.steps, 10))
-    D.set_stream(None)
+    e2e_steps = max(3, min(args.steps, 20))
     for _ in range(2):
         D.upload(*pn)
         D.step(1)
         D.download_into(on)
-    torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         D.upload(*pn)
@@ -291,7 +317,7 @@ def run_gb300(args, world, rank, local):
     traffic = None
     try:
         with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
-            traffic = json.load(f).get("update_kernel_dram_bytes")
+            traffic = json.load(f).get("update_kernel_dram_bytes_per_launch")
     except Exception:
         pass
 
@@ -325,6 +351,8 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cells", type=int, default=N_CELLS_SIDE, help="cells per side (profiling cases only)")
+    ap.add_argument("--profile", action="store_true", help="timed steps only (for ncu captures)")
     args = ap.parse_args()
     world, rank, local = dist_init()
     if args.impl == "reference":

@@ -101,6 +101,13 @@ int swe_gpu_upload_block(swe_gpu_domain *dom, int block, const float *h, const f
  * (SWE_Block::getWaterHeight & co., src/blocks/SWE_Block.hh:128-142). */
 int swe_gpu_download_block(swe_gpu_domain *dom, int block, float *h, float *hu, float *hv, float *b, int ld);
 
+/* Whole-domain transfers: host arrays hold every block's (nx+2)*(ny+2) floats
+ * in Float2D layout, blocks concatenated in rank order; NULL skips a field.
+ * One contiguous copy per field through a device staging buffer (pinned host
+ * memory reaches full link bandwidth).  Both return when the copy is done. */
+int swe_gpu_upload_domain(swe_gpu_domain *dom, const float *h, const float *hu, const float *hv, const float *b);
+int swe_gpu_download_domain(swe_gpu_domain *dom, float *h, float *hu, float *hv, float *b);
+
 /* bathymetry ghosts: OUTFLOW/WALL copies (SWE_Block::applyBoundaryBathymetry,
  * src/blocks/SWE_Block.hh:724-749) and neighbour copies (exchangeBathymetry,
  * src/blocks/SWE_DimensionalSplittingMpi.cpp:109-186; sendBathymetry,

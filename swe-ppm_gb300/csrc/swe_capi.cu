@@ -131,6 +131,32 @@ __global__ void solveEdgesKernel(long long n, const float *hL, const float *hR, 
     edgeSolve<S>(L, R, oHL[i], oHR[i], oHuL[i], oHuR[i], oS[i]);
 }
 
+/// Copies between the contiguous host-order layout (blocks concatenated, each
+/// (nx+2)*(ny+2) floats, a[x][y] = raw[x*(ny+2)+y]) in `stage` and the padded
+/// device layout of the current buffer; one CTA per column of one block.
+/// fieldMask bit f selects h, hu, hv, b; stage holds field f at f*stageElems.
+__global__ void repackKernel(const DomainDev d, float *stage, long long stageElems, int toDevice, int fieldMask,
+                             int blockOffset) {
+    const int k = blockIdx.y + blockOffset;
+    const BlockDesc B = d.blocks[k];
+    const int x = blockIdx.x;
+    if (x > B.nx + 1) return;
+    const int cur = d.groups[B.group].cur;
+    float *fields[4] = {cur ? d.h[1] : d.h[0], cur ? d.hu[1] : d.hu[0], cur ? d.hv[1] : d.hv[0], d.b};
+    const int rows = B.ny + 2;
+    for (int f = 0; f < 4; f++) {
+        if (!(fieldMask & (1 << f))) continue;
+        float *dev = fields[f] + B.base + size_t(x) * size_t(B.pitch);
+        float *st = stage + size_t(f) * size_t(stageElems) + size_t(B.stage) + size_t(x) * size_t(rows);
+        for (int y = threadIdx.x; y < rows; y += blockDim.x) {
+            if (toDevice)
+                dev[y] = st[y];
+            else
+                st[y] = dev[y];
+        }
+    }
+}
+
 } // namespace
 
 struct swe_gpu_domain {
@@ -150,6 +176,9 @@ struct swe_gpu_domain {
     WorkUnit *dUnits = nullptr;
     GroupState *dGroups = nullptr;
     DomainDev dev{};
+    float *stage = nullptr;       // host-order staging for transfers (4 fields)
+    long long stageElems = 0;     // floats per field in the staging layout
+    int maxCols = 0;              // max nx+2 over blocks
     cudaGraphExec_t graph = nullptr;
     int graphSteps = 0;
 };
@@ -204,6 +233,7 @@ void freeDomain(swe_gpu_domain *D) {
         cudaFree(D->hv[i]);
     }
     cudaFree(D->b);
+    cudaFree(D->stage);
     cudaFree(D->dBlocks);
     cudaFree(D->dUnits);
     cudaFree(D->dGroups);
@@ -292,6 +322,9 @@ int swe_gpu_domain_create(const swe_gpu_desc *desc, swe_gpu_domain **out) {
             B.bnd[s] = nb[s] >= 0 ? CONNECT_WITHIN_RANK : desc->boundary[s];
         }
         elems += size_t(B.nx + 2) * size_t(B.pitch);
+        B.stage = D->stageElems;
+        D->stageElems += (long long)(B.nx + 2) * (long long)(B.ny + 2);
+        D->maxCols = std::max(D->maxCols, B.nx + 2);
         D->maxPerimeter = std::max(D->maxPerimeter, 2 * B.nx + 2 * B.ny + 4);
         D->blocks.push_back(B);
     }
@@ -317,6 +350,7 @@ int swe_gpu_domain_create(const swe_gpu_desc *desc, swe_gpu_domain **out) {
         ok = cudaMalloc(&D->h[i], bytes) == cudaSuccess && cudaMalloc(&D->hu[i], bytes) == cudaSuccess &&
              cudaMalloc(&D->hv[i], bytes) == cudaSuccess;
     ok = ok && cudaMalloc(&D->b, bytes) == cudaSuccess;
+    ok = ok && cudaMalloc(&D->stage, sizeof(float) * 4 * size_t(D->stageElems)) == cudaSuccess;
     ok = ok && cudaMalloc(&D->dBlocks, sizeof(BlockDesc) * D->blocks.size()) == cudaSuccess;
     ok = ok && cudaMalloc(&D->dUnits, sizeof(WorkUnit) * D->units.size()) == cudaSuccess;
     ok = ok && cudaMalloc(&D->dGroups, sizeof(GroupState) * D->ngroups) == cudaSuccess;
@@ -378,39 +412,81 @@ int swe_gpu_block_shape(const swe_gpu_domain *dom, int block, int *nx, int *ny) 
     return SWE_GPU_OK;
 }
 
-static int transferBlock(swe_gpu_domain *D, int block, float *h, float *hu, float *hv, float *b, int ld, bool up) {
-    int rc = checkBlock(D, block);
-    if (rc) return rc;
-    const BlockDesc &B = D->blocks[block];
-    if (ld < B.ny + 2) return fail(SWE_GPU_ERR_INVALID, "ld %d < ny+2 = %d", ld, B.ny + 2);
+// Host <-> device transfers go through the staging buffer: large contiguous
+// copies at full link bandwidth, then a repack kernel that reads the current
+// buffer index on the device (so transfers need no host synchronisation
+// with queued steps).
+static int stageTransfer(swe_gpu_domain *D, int firstBlock, int nblocks, float *const host[4], int ld, bool up,
+                         bool wait) {
     CUDA_TRY(cudaSetDevice(D->device));
-    std::vector<GroupState> g;
-    rc = readGroups(D, g);
-    if (rc) return rc;
-    const int cur = g[B.group].cur;
-    float *dev[4] = {D->h[cur] + B.base, D->hu[cur] + B.base, D->hv[cur] + B.base, D->b + B.base};
-    float *host[4] = {h, hu, hv, b};
+    int mask = 0;
+    for (int f = 0; f < 4; f++)
+        if (host[f]) mask |= 1 << f;
+    if (!mask) return SWE_GPU_OK;
+    const BlockDesc &F = D->blocks[firstBlock];
+    const BlockDesc &L = D->blocks[firstBlock + nblocks - 1];
+    const long long n0 = F.stage;
+    const long long n = L.stage + (long long)(L.nx + 2) * (L.ny + 2) - n0;
+    const bool contiguous = (nblocks > 1) || ld == F.ny + 2;
+    const dim3 grid(unsigned(D->maxCols), unsigned(nblocks));
+    if (!up) {
+        repackKernel<<<grid, 256, 0, D->stream>>>(D->dev, D->stage, D->stageElems, 0, mask, firstBlock);
+        CUDA_TRY(cudaGetLastError());
+    }
     for (int f = 0; f < 4; f++) {
         if (!host[f]) continue;
-        if (up)
-            CUDA_TRY(cudaMemcpy2DAsync(dev[f], size_t(B.pitch) * 4, host[f], size_t(ld) * 4, size_t(B.ny + 2) * 4,
-                                       size_t(B.nx + 2), cudaMemcpyHostToDevice, D->stream));
-        else
-            CUDA_TRY(cudaMemcpy2DAsync(host[f], size_t(ld) * 4, dev[f], size_t(B.pitch) * 4, size_t(B.ny + 2) * 4,
-                                       size_t(B.nx + 2), cudaMemcpyDeviceToHost, D->stream));
+        float *st = D->stage + size_t(f) * size_t(D->stageElems) + size_t(n0);
+        if (contiguous) {
+            if (up)
+                CUDA_TRY(cudaMemcpyAsync(st, host[f], size_t(n) * 4, cudaMemcpyHostToDevice, D->stream));
+            else
+                CUDA_TRY(cudaMemcpyAsync(host[f], st, size_t(n) * 4, cudaMemcpyDeviceToHost, D->stream));
+        } else {
+            const size_t w = size_t(F.ny + 2) * 4;
+            if (up)
+                CUDA_TRY(cudaMemcpy2DAsync(st, w, host[f], size_t(ld) * 4, w, size_t(F.nx + 2), cudaMemcpyHostToDevice, D->stream));
+            else
+                CUDA_TRY(cudaMemcpy2DAsync(host[f], size_t(ld) * 4, st, w, w, size_t(F.nx + 2), cudaMemcpyDeviceToHost, D->stream));
+        }
     }
-    CUDA_TRY(cudaStreamSynchronize(D->stream));
+    if (up) {
+        repackKernel<<<grid, 256, 0, D->stream>>>(D->dev, D->stage, D->stageElems, 1, mask, firstBlock);
+        CUDA_TRY(cudaGetLastError());
+    }
+    if (wait) CUDA_TRY(cudaStreamSynchronize(D->stream));
     return SWE_GPU_OK;
 }
 
 int swe_gpu_upload_block(swe_gpu_domain *dom, int block, const float *h, const float *hu, const float *hv,
                          const float *b, int ld) {
-    return transferBlock(dom, block, const_cast<float *>(h), const_cast<float *>(hu), const_cast<float *>(hv),
-                         const_cast<float *>(b), ld, true);
+    int rc = checkBlock(dom, block);
+    if (rc) return rc;
+    if (ld < dom->blocks[block].ny + 2) return fail(SWE_GPU_ERR_INVALID, "ld %d < ny+2", ld);
+    float *const host[4] = {const_cast<float *>(h), const_cast<float *>(hu), const_cast<float *>(hv),
+                            const_cast<float *>(b)};
+    // the staging buffer is reused by the next transfer: wait for the copy
+    return stageTransfer(dom, block, 1, host, ld, true, true);
 }
 
 int swe_gpu_download_block(swe_gpu_domain *dom, int block, float *h, float *hu, float *hv, float *b, int ld) {
-    return transferBlock(dom, block, h, hu, hv, b, ld, false);
+    int rc = checkBlock(dom, block);
+    if (rc) return rc;
+    if (ld < dom->blocks[block].ny + 2) return fail(SWE_GPU_ERR_INVALID, "ld %d < ny+2", ld);
+    float *const host[4] = {h, hu, hv, b};
+    return stageTransfer(dom, block, 1, host, ld, false, true);
+}
+
+int swe_gpu_upload_domain(swe_gpu_domain *dom, const float *h, const float *hu, const float *hv, const float *b) {
+    if (!dom) return fail(SWE_GPU_ERR_INVALID, "null domain handle");
+    float *const host[4] = {const_cast<float *>(h), const_cast<float *>(hu), const_cast<float *>(hv),
+                            const_cast<float *>(b)};
+    return stageTransfer(dom, 0, int(dom->blocks.size()), host, 0, true, true);
+}
+
+int swe_gpu_download_domain(swe_gpu_domain *dom, float *h, float *hu, float *hv, float *b) {
+    if (!dom) return fail(SWE_GPU_ERR_INVALID, "null domain handle");
+    float *const host[4] = {h, hu, hv, b};
+    return stageTransfer(dom, 0, int(dom->blocks.size()), host, 0, false, true);
 }
 
 int swe_gpu_exchange_bathymetry(swe_gpu_domain *dom) {

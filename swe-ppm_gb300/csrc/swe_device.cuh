@@ -42,6 +42,7 @@ struct BlockDesc {
     int bnd[4];       // boundary types LEFT, RIGHT, BOTTOM, TOP
     int nbr[4];       // neighbour block ids (CONNECT_WITHIN_RANK) or -1
     float dx, dy;
+    long long stage;  // offset of the block in the contiguous host-order layout
 };
 
 // work unit of the sweep kernels: one block, rows [y0, y0+TY) x columns [x0, x1)

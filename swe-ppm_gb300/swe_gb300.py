@@ -37,7 +37,7 @@ SCENARIO_SHORELINE = 12
 
 EXPORTED = [
     "swe_gpu_domain_create", "swe_gpu_domain_destroy", "swe_gpu_block_count", "swe_gpu_block_shape",
-    "swe_gpu_upload_block", "swe_gpu_download_block", "swe_gpu_exchange_bathymetry", "swe_gpu_set_ghost_layer",
+    "swe_gpu_upload_block", "swe_gpu_download_block", "swe_gpu_upload_domain", "swe_gpu_download_domain", "swe_gpu_exchange_bathymetry", "swe_gpu_set_ghost_layer",
     "swe_gpu_compute_fluxes", "swe_gpu_update_unknowns", "swe_gpu_get_max_timestep", "swe_gpu_step",
     "swe_gpu_advance", "swe_gpu_get_time", "swe_gpu_set_time", "swe_gpu_sync", "swe_gpu_status",
     "swe_gpu_get_stream", "swe_gpu_set_stream", "swe_gpu_last_error", "swe_gpu_version", "swe_gpu_solve_edges",
@@ -82,6 +82,8 @@ def lib():
         L.swe_gpu_block_shape.argtypes = [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
         L.swe_gpu_upload_block.argtypes = [vp, C.c_int, vp, vp, vp, vp, C.c_int]
         L.swe_gpu_download_block.argtypes = [vp, C.c_int, vp, vp, vp, vp, C.c_int]
+        L.swe_gpu_upload_domain.argtypes = [vp, vp, vp, vp, vp]
+        L.swe_gpu_download_domain.argtypes = [vp, vp, vp, vp, vp]
         for n in ("swe_gpu_exchange_bathymetry", "swe_gpu_set_ghost_layer", "swe_gpu_compute_fluxes", "swe_gpu_sync"):
             getattr(L, n).argtypes = [vp]
         L.swe_gpu_update_unknowns.argtypes = [vp, C.c_float]
@@ -218,27 +220,40 @@ class Domain:
         except Exception:
             pass
 
+    def _arrs(self, arrs):
+        out = [None if a is None else np.ascontiguousarray(a, dtype=np.float32).ravel() for a in arrs]
+        for a in out:
+            if a is not None and a.size != self.ncells:
+                raise SweGpuError("array of %d values, domain has %d" % (a.size, self.ncells))
+        return out
+
     def upload(self, h=None, hu=None, hv=None, b=None):
+        """whole-domain upload (all blocks concatenated); None skips a field"""
+        _check(lib().swe_gpu_upload_domain(self.handle, *[_p(a) for a in self._arrs((h, hu, hv, b))]))
+
+    def upload_block(self, k, h=None, hu=None, hv=None, b=None):
+        nx, ny = self.shapes[k]
         arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float32).ravel() for a in (h, hu, hv, b)]
-        for k, (nx, ny) in enumerate(self.shapes):
-            o0, o1 = self.offsets[k], self.offsets[k + 1]
-            sl = [None if a is None else a[o0:o1] for a in arrs]
-            _check(lib().swe_gpu_upload_block(self.handle, k, *[_p(a) for a in sl], ny + 2))
+        _check(lib().swe_gpu_upload_block(self.handle, k, *[_p(a) for a in arrs], ny + 2))
 
     def download(self):
         arrs = [np.empty(self.ncells, dtype=np.float32) for _ in range(4)]
-        for k, (nx, ny) in enumerate(self.shapes):
-            o0, o1 = self.offsets[k], self.offsets[k + 1]
-            _check(lib().swe_gpu_download_block(self.handle, k, *[_p(a[o0:o1]) for a in arrs], ny + 2))
+        _check(lib().swe_gpu_download_domain(self.handle, *[_p(a) for a in arrs]))
+        return tuple(arrs)
+
+    def download_block(self, k):
+        nx, ny = self.shapes[k]
+        arrs = [np.empty((nx + 2) * (ny + 2), dtype=np.float32) for _ in range(4)]
+        _check(lib().swe_gpu_download_block(self.handle, k, *[_p(a) for a in arrs], ny + 2))
         return tuple(arrs)
 
     def download_into(self, arrs):
         """download h, hu, hv (and b if a 4th array is given) into preallocated float32 arrays"""
         arrs = list(arrs) + [None] * (4 - len(arrs))
-        for k, (nx, ny) in enumerate(self.shapes):
-            o0, o1 = self.offsets[k], self.offsets[k + 1]
-            _check(lib().swe_gpu_download_block(self.handle, k, *[None if a is None else _p(a[o0:o1]) for a in arrs],
-                                                ny + 2))
+        for a in arrs:
+            if a is not None and (a.dtype != np.float32 or a.size != self.ncells or not a.flags.c_contiguous):
+                raise SweGpuError("download_into needs contiguous float32 arrays of the domain size")
+        _check(lib().swe_gpu_download_domain(self.handle, *[_p(a) for a in arrs]))
 
     def exchange_bathymetry(self):
         _check(lib().swe_gpu_exchange_bathymetry(self.handle))

@@ -183,3 +183,38 @@ def test_nan_state_sets_status_flag(swe):
     with pytest.raises(swe.SweGpuError):
         D.advance(1.0, max_steps=2)
     D.close()
+
+
+def test_per_block_transfers_with_padded_rows(swe, oracle_mod):
+    """swe_gpu_upload_block / swe_gpu_download_block with a column stride ld >
+    ny+2 (caller-owned Float2D-like arrays) round-trip and step like the
+    whole-domain path."""
+    geo, h0, hu0, hv0, b0 = swe.init_domain(1, 70, 45, 6, [])
+    D = swe.Domain(geo["nx_cols"], geo["ny_rows"], geo["dx"], geo["dy"], boundary=geo["boundary"], solver=4)
+    off = 0
+    for k, (nx, ny) in enumerate(D.shapes):
+        n = (nx + 2) * (ny + 2)
+        ld = ny + 2 + 5
+        padded = []
+        for a in (h0, hu0, hv0, b0):
+            p = np.full((nx + 2, ld), np.nan, dtype=np.float32)
+            p[:, :ny + 2] = a[off:off + n].reshape(nx + 2, ny + 2)
+            padded.append(p)
+        import ctypes
+        rc = swe.lib().swe_gpu_upload_block(D.handle, k, *[p.ctypes.data_as(ctypes.c_void_p) for p in padded], ld)
+        assert rc == 0
+        off += n
+    D.exchange_bathymetry()
+    D.step(5)
+    D.sync()
+    out = D.download()
+    R = oracle_mod.Domain(geo["nx_cols"], geo["ny_rows"], geo["dx"], geo["dy"], outer=geo["boundary"], solver=4)
+    R.set_state(h0, hu0, hv0, b0)
+    R.bathymetry_ghosts()
+    R.step(5)
+    compare(out, R.get_state(), "per-block upload")
+    blk = D.download_block(3)
+    o0, o1 = D.offsets[3], D.offsets[4]
+    for a, b_ in zip(blk, out):
+        assert_bitwise(a, b_[o0:o1], "download_block")
+    D.close()
