@@ -480,13 +480,13 @@ int swe_gpu_upload_domain(swe_gpu_domain *dom, const float *h, const float *hu, 
     if (!dom) return fail(SWE_GPU_ERR_INVALID, "null domain handle");
     float *const host[4] = {const_cast<float *>(h), const_cast<float *>(hu), const_cast<float *>(hv),
                             const_cast<float *>(b)};
-    return stageTransfer(dom, 0, int(dom->blocks.size()), host, 0, true, true);
+    return stageTransfer(dom, 0, int(dom->blocks.size()), host, dom->blocks[0].ny + 2, true, true);
 }
 
 int swe_gpu_download_domain(swe_gpu_domain *dom, float *h, float *hu, float *hv, float *b) {
     if (!dom) return fail(SWE_GPU_ERR_INVALID, "null domain handle");
     float *const host[4] = {h, hu, hv, b};
-    return stageTransfer(dom, 0, int(dom->blocks.size()), host, 0, false, true);
+    return stageTransfer(dom, 0, int(dom->blocks.size()), host, dom->blocks[0].ny + 2, false, true);
 }
 
 int swe_gpu_exchange_bathymetry(swe_gpu_domain *dom) {
