@@ -156,6 +156,29 @@ int swe_gpu_solve_edges(int solver, long long n, const float *hL, const float *h
                         const float *huR, const float *bL, const float *bR, float *hUpdL, float *hUpdR,
                         float *huUpdL, float *huUpdR, float *maxWaveSpeed, void *stream);
 
+/* Allocation-free step of one block -- no counterpart in the reference.
+ * For callers that cannot allocate device memory: hosts whose GPU memory
+ * belongs to another allocator (a framework's caching pool, a fixed arena)
+ * and latency-critical loops that cannot take cudaMalloc's implicit device
+ * synchronisation.  Runs setGhostLayer + computeNumericalFluxes +
+ * updateUnknowns of one block (solver, semantics as above; split semantics
+ * reduce dt with SWE_SPLIT_DT_MAX) on caller-owned DEVICE arrays in Float2D
+ * layout with column stride ld >= ny+2: h, hu, hv hold Q^n (their ghost cells
+ * are written, like setGhostLayer), b the bathymetry with its ghosts,
+ * h_out/hu_out/hv_out receive Q^{n+1} (ghost ring carried over) and must not
+ * alias the inputs.  If dt_out (host) is not NULL the call waits for the
+ * stream and stores the step's dt there.  Nothing is allocated: the scratch
+ * (dt control block, block descriptor, CTA work list) is a fixed array of
+ * about 66 KB that every GPU loading the library holds until exit, so the
+ * block may need at most 4096 work units, ceil(ny/256) * ceil(nx/32); larger
+ * blocks are rejected with SWE_GPU_ERR_INVALID.  The first call on a device
+ * looks the array's device address up (cudaGetSymbolAddress); make that first
+ * call before any stream capture.  Every call on a device shares the array and
+ * clears it when it starts: calls that overlap on the GPU race. */
+int swe_gpu_step_block_noalloc(int solver, int semantics, int nx, int ny, float dx, float dy, const int *boundary4,
+                               int ld, float *h, float *hu, float *hv, const float *b, float *h_out, float *hu_out,
+                               float *hv_out, float *dt_out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -7,6 +7,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -654,3 +655,154 @@ int swe_gpu_solve_edges(int solver, long long n, const float *hL, const float *h
 }
 
 } // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free single-block step.
+//
+// Some callers cannot allocate device memory: hosts whose GPU memory is owned
+// by another allocator (a framework's caching pool or a pre-sized arena that
+// must not grow), and latency-critical loops that cannot afford cudaMalloc's
+// implicit device-wide synchronisation.  swe_gpu_step_block_noalloc runs one
+// step of one block on the caller's device arrays and keeps the little scratch
+// the step kernels need (the dt control block, the block descriptor and the
+// CTA work list) in the file-scope array below instead of allocating it.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr int kNoAllocMaxUnits = 4096;  // CTA work units: (ny/256 rounded up) * (nx/32 rounded up)
+constexpr int kNoAllocMaxDevices = 64;
+
+struct NoAllocScratch {
+    GroupState group;
+    BlockDesc block;
+    WorkUnit units[kNoAllocMaxUnits];
+};
+
+} // namespace
+
+// One copy per GPU that loads the library, held until the process exits
+// (about 66 KB).  Every call on a device reuses it: the set-up kernel below
+// clears the control block at the start of each call, and calls that overlap
+// on the GPU (different streams, or several host threads) race on it.
+static __device__ __align__(256) NoAllocScratch g_noallocScratch;
+
+namespace {
+
+std::mutex g_noallocMutex;
+NoAllocScratch *g_noallocPtr[kNoAllocMaxDevices] = {};
+
+/// Device address of the scratch array for `device` (current device), looked
+/// up once per device; in host code the symbol itself is only a stand-in.
+int noallocScratch(int device, NoAllocScratch **out) {
+    if (device < 0 || device >= kNoAllocMaxDevices)
+        return fail(SWE_GPU_ERR_INVALID, "device %d beyond the %d supported", device, kNoAllocMaxDevices);
+    std::lock_guard<std::mutex> lock(g_noallocMutex);
+    if (!g_noallocPtr[device]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noallocScratch);
+        if (e != cudaSuccess)
+            return fail(SWE_GPU_ERR_CUDA, "cudaGetSymbolAddress(scratch): %s", cudaGetErrorString(e));
+        g_noallocPtr[device] = static_cast<NoAllocScratch *>(p);
+    }
+    *out = g_noallocPtr[device];
+    return SWE_GPU_OK;
+}
+
+/// writes the block descriptor and work list and clears the control block
+__global__ void noallocSetupKernel(NoAllocScratch *s, BlockDesc b, int tileRows, int tileCols, int nunits) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) {
+        GroupState g;
+        g.speedBits = 0u;
+        g.arrived = 0u;
+        g.units = nunits;
+        g.firstBlock = 0;
+        g.dt = 0.f;
+        g.speed = 0.f;
+        g.time = 0.f;
+        g.target = INFINITY;
+        g.steps = 0;
+        g.cur = 0;
+        g.status = 0;
+        g.pad = 0;
+        s->group = g;
+        s->block = b;
+    }
+    const int xChunks = (b.nx + tileCols - 1) / tileCols;
+    for (int u = i; u < nunits; u += gridDim.x * blockDim.x) {
+        const int ty = u / xChunks, xc = u % xChunks;
+        s->units[u] = WorkUnit{0, 1 + ty * tileRows, 1 + xc * tileCols, min(1 + (xc + 1) * tileCols, b.nx + 1)};
+    }
+}
+
+} // namespace
+
+extern "C" int swe_gpu_step_block_noalloc(int solver, int semantics, int nx, int ny, float dx, float dy,
+                                          const int *boundary, int ld, float *h, float *hu, float *hv,
+                                          const float *b, float *h_out, float *hu_out, float *hv_out,
+                                          float *dt_out, void *stream) {
+    if (solver < SWE_SOLVER_FWAVE || solver > SWE_SOLVER_HLLE) return fail(SWE_GPU_ERR_INVALID, "unknown solver %d", solver);
+    if (semantics != SWE_SEMANTICS_UNSPLIT && semantics != SWE_SEMANTICS_SPLIT)
+        return fail(SWE_GPU_ERR_INVALID, "unknown semantics %d", semantics);
+    if (nx < 1 || ny < 1) return fail(SWE_GPU_ERR_INVALID, "block size %d x %d", nx, ny);
+    if (!(dx > 0.f) || !(dy > 0.f)) return fail(SWE_GPU_ERR_INVALID, "dx, dy must be positive");
+    if (ld < ny + 2) return fail(SWE_GPU_ERR_INVALID, "ld %d < ny+2 = %d", ld, ny + 2);
+    if (!boundary || !h || !hu || !hv || !b || !h_out || !hu_out || !hv_out)
+        return fail(SWE_GPU_ERR_INVALID, "null array argument");
+    for (int i = 0; i < 4; i++)
+        if (boundary[i] < SWE_OUTFLOW || boundary[i] > SWE_PASSIVE || boundary[i] == SWE_CONNECT_WITHIN_RANK)
+            return fail(SWE_GPU_ERR_INVALID, "boundary %d: type %d is not valid for a single block", i, boundary[i]);
+    const int tileRows = std::min(256, ((ny + 31) / 32) * 32);
+    const int tileCols = 32;
+    const long long nunits = (long long)((ny + tileRows - 1) / tileRows) * ((nx + tileCols - 1) / tileCols);
+    if (nunits > kNoAllocMaxUnits)
+        return fail(SWE_GPU_ERR_INVALID,
+                    "block %d x %d needs %lld work units; the allocation-free step supports at most %d "
+                    "(ceil(ny/256) * ceil(nx/32))", nx, ny, nunits, kNoAllocMaxUnits);
+    int device = 0;
+    CUDA_TRY(cudaGetDevice(&device));
+    NoAllocScratch *scr = nullptr;
+    int rc = noallocScratch(device, &scr);
+    if (rc) return rc;
+
+    BlockDesc B{};
+    B.nx = nx;
+    B.ny = ny;
+    B.pitch = ld;
+    B.group = 0;
+    B.base = 0;
+    B.dx = dx;
+    B.dy = dy;
+    B.stage = 0;
+    for (int i = 0; i < 4; i++) {
+        B.bnd[i] = boundary[i];
+        B.nbr[i] = -1;
+    }
+    DomainDev d{};
+    d.h[0] = h; d.h[1] = h_out;
+    d.hu[0] = hu; d.hu[1] = hu_out;
+    d.hv[0] = hv; d.hv[1] = hv_out;
+    d.b = const_cast<float *>(b);
+    d.blocks = &scr->block;
+    d.units = scr->units;
+    d.groups = &scr->group;
+    d.nblocks = 1;
+    d.solver = solver;
+    d.semantics = semantics;
+    d.splitDtMode = SPLIT_DT_MAX;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+
+    noallocSetupKernel<<<(unsigned)std::max<long long>(1, std::min<long long>(64, (nunits + 255) / 256)), 256, 0, s>>>(
+        scr, B, tileRows, tileCols, int(nunits));
+    CUDA_TRY(cudaGetLastError());
+    const int threads = 128;
+    ghostKernel<<<dim3((2 * nx + 2 * ny + 4 + threads - 1) / threads, 1), threads, 0, s>>>(d, 0);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(launchSpeed(d, int(nunits), tileRows, s));
+    CUDA_TRY(launchUpdate(d, int(nunits), tileRows, s));
+    if (dt_out) {
+        CUDA_TRY(cudaMemcpyAsync(dt_out, &scr->group.dt, sizeof(float), cudaMemcpyDeviceToHost, s));
+        CUDA_TRY(cudaStreamSynchronize(s));
+    }
+    return SWE_GPU_OK;
+}

@@ -40,7 +40,7 @@ EXPORTED = [
     "swe_gpu_upload_block", "swe_gpu_download_block", "swe_gpu_upload_domain", "swe_gpu_download_domain", "swe_gpu_exchange_bathymetry", "swe_gpu_set_ghost_layer",
     "swe_gpu_compute_fluxes", "swe_gpu_update_unknowns", "swe_gpu_get_max_timestep", "swe_gpu_step",
     "swe_gpu_advance", "swe_gpu_get_time", "swe_gpu_set_time", "swe_gpu_sync", "swe_gpu_status",
-    "swe_gpu_get_stream", "swe_gpu_set_stream", "swe_gpu_last_error", "swe_gpu_version", "swe_gpu_solve_edges",
+    "swe_gpu_get_stream", "swe_gpu_set_stream", "swe_gpu_last_error", "swe_gpu_version", "swe_gpu_solve_edges", "swe_gpu_step_block_noalloc",
     "swe_host_scenario_geometry", "swe_host_scenario_boundary", "swe_host_init_block", "swe_host_decompose",
 ]
 
@@ -96,6 +96,8 @@ def lib():
         L.swe_gpu_get_stream.argtypes = [vp, C.POINTER(vp)]
         L.swe_gpu_set_stream.argtypes = [vp, vp]
         L.swe_gpu_solve_edges.argtypes = [C.c_int, C.c_longlong] + [vp] * 11 + [vp]
+        L.swe_gpu_step_block_noalloc.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, vp,
+                                                 C.c_int] + [vp] * 7 + [vp, vp]
         L.swe_host_scenario_geometry.argtypes = [C.c_int, vp, C.c_int, C.c_int, vp]
         L.swe_host_scenario_boundary.argtypes = [C.c_int, vp, vp]
         L.swe_host_init_block.argtypes = [C.c_int, vp, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float,
@@ -310,3 +312,15 @@ def solve_edges_device(solver, ptrs_in, ptrs_out, n, stream=None):
     """Per-edge solver on device pointers (6 inputs, 5 outputs)."""
     _check(lib().swe_gpu_solve_edges(int(solver), int(n), *[C.c_void_p(p) for p in ptrs_in],
                                      *[C.c_void_p(p) for p in ptrs_out], C.c_void_p(stream or 0)))
+
+
+def step_block_noalloc(solver, semantics, nx, ny, dx, dy, boundary, ld, ins, outs, stream=None, want_dt=True):
+    """Allocation-free step of one block on device pointers: ins = (h, hu, hv, b),
+    outs = (h_out, hu_out, hv_out); returns dt when want_dt (the call then waits)."""
+    bnd = (C.c_int * 4)(*[int(v) for v in boundary])
+    dt = C.c_float()
+    _check(lib().swe_gpu_step_block_noalloc(int(solver), int(semantics), int(nx), int(ny), float(dx), float(dy),
+                                            C.cast(bnd, C.c_void_p), int(ld), *[C.c_void_p(p) for p in ins],
+                                            *[C.c_void_p(p) for p in outs], C.byref(dt) if want_dt else None,
+                                            C.c_void_p(stream or 0)))
+    return dt.value if want_dt else None
