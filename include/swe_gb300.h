@@ -165,11 +165,11 @@ int swe_gpu_solve_edges(int solver, long long n, const float *hL, const float *h
  * reduce dt with SWE_SPLIT_DT_MAX) on caller-owned DEVICE arrays in Float2D
  * layout with column stride ld >= ny+2: h, hu, hv hold Q^n (their ghost cells
  * are written, like setGhostLayer), b the bathymetry with its ghosts,
- * h_out/hu_out/hv_out receive Q^{n+1} (ghost ring carried over) and must not
- * alias the inputs.  If dt_out (host) is not NULL the call waits for the
+ * h_out/hu_out/hv_out receive Q^{n+1} with its ghost ring already set for
+ * the next step, and must not alias the inputs.  If dt_out (host) is not NULL the call waits for the
  * stream and stores the step's dt there.  Nothing is allocated: the scratch
  * (dt control block, block descriptor, CTA work list) is a fixed array of
- * about 66 KB that every GPU loading the library holds until exit, so the
+ * about 82 KB that every GPU loading the library holds until exit, so the
  * block may need at most 4096 work units, ceil(ny/256) * ceil(nx/32); larger
  * blocks are rejected with SWE_GPU_ERR_INVALID.  The first call on a device
  * looks the array's device address up (cudaGetSymbolAddress); make that first

@@ -43,8 +43,9 @@ public:
             huR = -huL;
             bR = bL;
         }
-        const T uL = huL / hL;
-        const T uR = huR / hR;
+        // per-cell quantities: one division and one square root per cell
+        const T uL = huL * (T(1) / hL);
+        const T uR = huR * (T(1) / hR);
         const T sqL = std::sqrt(hL);
         const T sqR = std::sqrt(hR);
         const T uRoe = detail::roeVelocity(uL, uR, sqL, sqR);

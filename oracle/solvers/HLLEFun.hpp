@@ -24,7 +24,7 @@ namespace solver {
 template <typename T> class HLLEFun {
 public:
     explicit HLLEFun(T dryTol = T(0.01), T gravity = T(9.81), T zeroTol = T(1e-7))
-        : dryTol_(dryTol), g_(gravity), zeroTol_(zeroTol) {}
+        : dryTol_(dryTol), g_(gravity), zeroTol_(zeroTol), sqrtG_(std::sqrt(gravity)) {}
 
     void computeNetUpdates(T hL, T hR, T huL, T huR, T bL, T bR,
                            T &hUpdL, T &hUpdR, T &huUpdL, T &huUpdR, T &maxWaveSpeed) const {
@@ -44,12 +44,13 @@ public:
             huR = -huL;
             bR = bL;
         }
-        const T uL = huL / hL;
-        const T uR = huR / hR;
+        // per-cell quantities: one division and one square root per cell
+        const T uL = huL * (T(1) / hL);
+        const T uR = huR * (T(1) / hR);
         const T sqL = std::sqrt(hL);
         const T sqR = std::sqrt(hR);
-        const T cL = std::sqrt(g_ * hL);
-        const T cR = std::sqrt(g_ * hR);
+        const T cL = sqrtG_ * sqL;  // sqrt(g h) as sqrt(g) * sqrt(h)
+        const T cR = sqrtG_ * sqR;
         const T uRoe = detail::roeVelocity(uL, uR, sqL, sqR);
         const T cRoe = std::sqrt(g_ * (T(0.5) * (hL + hR)));
         const T s1 = detail::vmin(uL - cL, uRoe - cRoe);
@@ -70,7 +71,7 @@ public:
     }
 
 private:
-    T dryTol_, g_, zeroTol_;
+    T dryTol_, g_, zeroTol_, sqrtG_;
 };
 
 } // namespace solver

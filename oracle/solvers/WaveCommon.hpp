@@ -15,6 +15,10 @@
  * Parity of the solver arithmetic is therefore unpinned; the block code around
  * it is pinned bit-for-bit against the reference's own compiled sources.
  *
+ * Per-cell quantities of the f-wave and HLLE solvers are formed as
+ * u = hu * (1/h) and sqrt(g h) = sqrt(g) * sqrt(h): one division and one
+ * square root per cell, so a GPU can share them between a cell's four edges.
+ *
  * Floating-point contract: every multiply-add that is fused is written as an
  * explicit std::fma; everything else is a separate IEEE operation. Build with
  * -ffp-contract=off and without -ffast-math to get results that are identical

@@ -52,6 +52,8 @@ __global__ void ghostKernel(const DomainDev d, int bathymetry) {
     const int nx = B.nx, ny = B.ny;
     const size_t P = size_t(B.pitch);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    // the ghost ring of the current buffer now belongs to the current state
+    if (!bathymetry && threadIdx.x == 0) const_cast<GroupState *>(G)->ghostsAhead = 0;
     float *fields[3];
     int nf;
     if (bathymetry) {
@@ -125,10 +127,11 @@ __global__ void solveEdgesKernel(long long n, const float *hL, const float *hR, 
     Cell L, R;
     L.h = a; L.hn = e; L.b = bL[i];
     R.h = c; R.hn = f; R.b = bR[i];
-    L.u = (a < kDryTol) ? 0.f : e / a;
-    R.u = (c < kDryTol) ? 0.f : f / c;
+    // per-cell quantities as the sweep kernels form them
+    L.u = (a < kDryTol) ? 0.f : e * (1.f / a);
+    R.u = (c < kDryTol) ? 0.f : f * (1.f / c);
     L.sq = sqrtf(a); R.sq = sqrtf(c);
-    L.c = sqrtf(kG * a); R.c = sqrtf(kG * c);
+    L.c = kSqrtG * L.sq; R.c = kSqrtG * R.sq;
     edgeSolve<S>(L, R, oHL[i], oHR[i], oHuL[i], oHuR[i], oS[i]);
 }
 
@@ -142,18 +145,29 @@ __global__ void repackKernel(const DomainDev d, float *stage, long long stageEle
     const BlockDesc B = d.blocks[k];
     const int x = blockIdx.x;
     if (x > B.nx + 1) return;
-    const int cur = d.groups[B.group].cur;
+    GroupState *G = d.groups + B.group;
+    const int cur = G->cur;
+    // After an update pass the current buffer's ghost ring already holds the
+    // next step's boundary values; the block's state as the reference shows
+    // it (ghosts set at the start of the last step) has them in the other buffer.
+    const bool ahead = !toDevice && G->ghostsAhead;
+    if (toDevice && x == 0 && threadIdx.x == 0) G->ghostsAhead = 0;
     float *fields[4] = {cur ? d.h[1] : d.h[0], cur ? d.hu[1] : d.hu[0], cur ? d.hv[1] : d.hv[0], d.b};
+    float *other[4] = {cur ? d.h[0] : d.h[1], cur ? d.hu[0] : d.hu[1], cur ? d.hv[0] : d.hv[1], d.b};
     const int rows = B.ny + 2;
+    const bool ghostColumn = (x == 0) || (x == B.nx + 1);
     for (int f = 0; f < 4; f++) {
         if (!(fieldMask & (1 << f))) continue;
         float *dev = fields[f] + B.base + size_t(x) * size_t(B.pitch);
+        float *oth = other[f] + B.base + size_t(x) * size_t(B.pitch);
         float *st = stage + size_t(f) * size_t(stageElems) + size_t(B.stage) + size_t(x) * size_t(rows);
         for (int y = threadIdx.x; y < rows; y += blockDim.x) {
-            if (toDevice)
+            if (toDevice) {
                 dev[y] = st[y];
-            else
-                st[y] = dev[y];
+            } else {
+                const bool ghost = ghostColumn || y == 0 || y == rows - 1;
+                st[y] = (ahead && ghost) ? oth[y] : dev[y];
+            }
         }
     }
 }
@@ -175,7 +189,11 @@ struct swe_gpu_domain {
     float *h[2] = {nullptr, nullptr}, *hu[2] = {nullptr, nullptr}, *hv[2] = {nullptr, nullptr}, *b = nullptr;
     BlockDesc *dBlocks = nullptr;
     WorkUnit *dUnits = nullptr;
+    int *dCtaSeg = nullptr;
     GroupState *dGroups = nullptr;
+    std::vector<int> ctaSeg;      // CTA c owns segments [ctaSeg[c], ctaSeg[c+1])
+    int grid = 0;                 // CTAs of the sweep kernels
+    bool ghostsValid = false;     // the current buffer's ghost ring matches its interior
     DomainDev dev{};
     float *stage = nullptr;       // host-order staging for transfers (4 fields)
     long long stageElems = 0;     // floats per field in the staging layout
@@ -195,19 +213,25 @@ int enqueueGhost(swe_gpu_domain *D, int bathymetry) {
 }
 
 int enqueueSpeed(swe_gpu_domain *D) {
-    CUDA_TRY(launchSpeed(D->dev, int(D->units.size()), D->tileRows, D->stream));
+    CUDA_TRY(launchSpeed(D->dev, D->grid, D->tileRows, D->stream));
     return SWE_GPU_OK;
 }
 
 int enqueueUpdate(swe_gpu_domain *D) {
-    CUDA_TRY(launchUpdate(D->dev, int(D->units.size()), D->tileRows, D->stream));
+    CUDA_TRY(launchUpdate(D->dev, D->grid, D->tileRows, D->stream));
+    D->ghostsValid = true;  // the update pass pushed the next ghost ring
     return SWE_GPU_OK;
 }
 
+/// one fused step; the ghost kernel runs only when the ghost ring is stale
+/// (after an upload), every update pass leaves a valid one behind
 int enqueueStep(swe_gpu_domain *D) {
-    int rc = enqueueGhost(D, 0);
-    if (rc) return rc;
-    rc = enqueueSpeed(D);
+    if (!D->ghostsValid) {
+        int rc = enqueueGhost(D, 0);
+        if (rc) return rc;
+        D->ghostsValid = true;
+    }
+    int rc = enqueueSpeed(D);
     if (rc) return rc;
     return enqueueUpdate(D);
 }
@@ -237,6 +261,7 @@ void freeDomain(swe_gpu_domain *D) {
     cudaFree(D->stage);
     cudaFree(D->dBlocks);
     cudaFree(D->dUnits);
+    cudaFree(D->dCtaSeg);
     cudaFree(D->dGroups);
     if (D->ownStream) cudaStreamDestroy(D->ownStream);
     delete D;
@@ -331,11 +356,42 @@ int swe_gpu_domain_create(const swe_gpu_desc *desc, swe_gpu_domain **out) {
     }
     elems += 32;  // slack so the last column's padding stays inside the allocation
     D->fieldElems = elems;
-    for (int k = 0; k < int(D->blocks.size()); k++) {
-        const BlockDesc &B = D->blocks[k];
-        for (int y0 = 1; y0 <= B.ny; y0 += D->tileRows)
-            for (int x0 = 1; x0 <= B.nx; x0 += D->tileCols)
-                D->units.push_back(WorkUnit{k, y0, x0, std::min(x0 + D->tileCols, B.nx + 1)});
+    // Balanced persistent partition: the (row tile, column) pairs of all blocks
+    // in order, split into `grid` equal runs; a run that crosses a tile or a
+    // block boundary becomes several segments.  tile_cols, when given, caps
+    // the segment length.
+    {
+        int sms = 148;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, D->device);
+        const int perSM = std::max(1, std::min(16, stepOccupancy(D->solver, D->semantics, D->tileRows)));
+        long long total = 0;
+        for (const BlockDesc &B : D->blocks) total += (long long)((B.ny + D->tileRows - 1) / D->tileRows) * B.nx;
+        const long long want = desc->tile_cols > 0 ? (total + desc->tile_cols - 1) / desc->tile_cols : (long long)sms * perSM;
+        D->grid = int(std::max(1LL, std::min(total, std::max(want, (long long)sms * perSM))));
+        D->ctaSeg.assign(1, 0);
+        long long pos = 0;  // global (tile, column) index
+        int k = 0, tile = 0, col = 1;
+        auto tiles = [&](int kk) { return (D->blocks[kk].ny + D->tileRows - 1) / D->tileRows; };
+        for (int c = 0; c < D->grid; c++) {
+            long long end = total * (c + 1) / D->grid;
+            while (pos < end) {
+                const BlockDesc &B = D->blocks[k];
+                const long long take = std::min<long long>(end - pos, (long long)(B.nx + 1 - col));
+                const int cap = desc->tile_cols > 0 ? desc->tile_cols : kMaxTileCols;
+                const int len = int(std::min<long long>(take, cap));
+                D->units.push_back(WorkUnit{k, 1 + tile * D->tileRows, col, col + len});
+                pos += len;
+                col += len;
+                if (col > B.nx) {
+                    col = 1;
+                    if (++tile >= tiles(k)) {
+                        tile = 0;
+                        k++;
+                    }
+                }
+            }
+            D->ctaSeg.push_back(int(D->units.size()));
+        }
     }
     GroupState g0{};
     g0.units = int(D->units.size());
@@ -354,6 +410,7 @@ int swe_gpu_domain_create(const swe_gpu_desc *desc, swe_gpu_domain **out) {
     ok = ok && cudaMalloc(&D->stage, sizeof(float) * 4 * size_t(D->stageElems)) == cudaSuccess;
     ok = ok && cudaMalloc(&D->dBlocks, sizeof(BlockDesc) * D->blocks.size()) == cudaSuccess;
     ok = ok && cudaMalloc(&D->dUnits, sizeof(WorkUnit) * D->units.size()) == cudaSuccess;
+    ok = ok && cudaMalloc(&D->dCtaSeg, sizeof(int) * D->ctaSeg.size()) == cudaSuccess;
     ok = ok && cudaMalloc(&D->dGroups, sizeof(GroupState) * D->ngroups) == cudaSuccess;
     if (!ok) {
         cudaGetLastError();
@@ -368,6 +425,7 @@ int swe_gpu_domain_create(const swe_gpu_desc *desc, swe_gpu_domain **out) {
     cudaMemsetAsync(D->b, 0, bytes, D->stream);
     cudaMemcpyAsync(D->dBlocks, D->blocks.data(), sizeof(BlockDesc) * D->blocks.size(), cudaMemcpyHostToDevice, D->stream);
     cudaMemcpyAsync(D->dUnits, D->units.data(), sizeof(WorkUnit) * D->units.size(), cudaMemcpyHostToDevice, D->stream);
+    cudaMemcpyAsync(D->dCtaSeg, D->ctaSeg.data(), sizeof(int) * D->ctaSeg.size(), cudaMemcpyHostToDevice, D->stream);
     cudaMemcpyAsync(D->dGroups, D->groupsInit.data(), sizeof(GroupState) * D->ngroups, cudaMemcpyHostToDevice, D->stream);
     e = cudaStreamSynchronize(D->stream);
     if (e != cudaSuccess) {
@@ -382,6 +440,7 @@ int swe_gpu_domain_create(const swe_gpu_desc *desc, swe_gpu_domain **out) {
     D->dev.b = D->b;
     D->dev.blocks = D->dBlocks;
     D->dev.units = D->dUnits;
+    D->dev.ctaSeg = D->dCtaSeg;
     D->dev.groups = D->dGroups;
     D->dev.nblocks = int(D->blocks.size());
     D->dev.solver = D->solver;
@@ -453,6 +512,7 @@ static int stageTransfer(swe_gpu_domain *D, int firstBlock, int nblocks, float *
     if (up) {
         repackKernel<<<grid, 256, 0, D->stream>>>(D->dev, D->stage, D->stageElems, 1, mask, firstBlock);
         CUDA_TRY(cudaGetLastError());
+        D->ghostsValid = false;
     }
     if (wait) CUDA_TRY(cudaStreamSynchronize(D->stream));
     return SWE_GPU_OK;
@@ -499,7 +559,9 @@ int swe_gpu_exchange_bathymetry(swe_gpu_domain *dom) {
 int swe_gpu_set_ghost_layer(swe_gpu_domain *dom) {
     if (!dom) return fail(SWE_GPU_ERR_INVALID, "null domain handle");
     CUDA_TRY(cudaSetDevice(dom->device));
-    return enqueueGhost(dom, 0);
+    int rc = enqueueGhost(dom, 0);
+    if (!rc) dom->ghostsValid = true;
+    return rc;
 }
 
 int swe_gpu_compute_fluxes(swe_gpu_domain *dom) {
@@ -676,12 +738,13 @@ struct NoAllocScratch {
     GroupState group;
     BlockDesc block;
     WorkUnit units[kNoAllocMaxUnits];
+    int ctaSeg[kNoAllocMaxUnits + 1];
 };
 
 } // namespace
 
 // One copy per GPU that loads the library, held until the process exits
-// (about 66 KB).  Every call on a device reuses it: the set-up kernel below
+// (about 82 KB).  Every call on a device reuses it: the set-up kernel below
 // clears the control block at the start of each call, and calls that overlap
 // on the GPU (different streams, or several host threads) race on it.
 static __device__ __align__(256) NoAllocScratch g_noallocScratch;
@@ -724,7 +787,7 @@ __global__ void noallocSetupKernel(NoAllocScratch *s, BlockDesc b, int tileRows,
         g.steps = 0;
         g.cur = 0;
         g.status = 0;
-        g.pad = 0;
+        g.ghostsAhead = 0;
         s->group = g;
         s->block = b;
     }
@@ -732,7 +795,9 @@ __global__ void noallocSetupKernel(NoAllocScratch *s, BlockDesc b, int tileRows,
     for (int u = i; u < nunits; u += gridDim.x * blockDim.x) {
         const int ty = u / xChunks, xc = u % xChunks;
         s->units[u] = WorkUnit{0, 1 + ty * tileRows, 1 + xc * tileCols, min(1 + (xc + 1) * tileCols, b.nx + 1)};
+        s->ctaSeg[u] = u;  // one segment per CTA
     }
+    if (i == 0) s->ctaSeg[nunits] = nunits;
 }
 
 } // namespace
@@ -785,6 +850,7 @@ extern "C" int swe_gpu_step_block_noalloc(int solver, int semantics, int nx, int
     d.b = const_cast<float *>(b);
     d.blocks = &scr->block;
     d.units = scr->units;
+    d.ctaSeg = scr->ctaSeg;
     d.groups = &scr->group;
     d.nblocks = 1;
     d.solver = solver;

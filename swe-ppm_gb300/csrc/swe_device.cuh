@@ -23,6 +23,7 @@ namespace swegb {
 
 constexpr float kG = 9.81f;
 constexpr float kHalfG = 0.5f * 9.81f;  // exact in float
+constexpr float kSqrtG = 0x1.90e864p+1f;  // sqrtf(9.81f), correctly rounded
 constexpr float kDryTol = 0.01f;        // solver dry tolerance
 constexpr float kZeroTol = 1e-7f;       // |s| below this: wave split evenly
 constexpr int kColPad = 31;             // y = 0 sits at offset 31 of a column
@@ -67,14 +68,16 @@ struct GroupState {
     int steps;               // executed steps
     int cur;                 // buffer (0/1) holding the current state
     int status;              // bit 0: NaN wave speed, bit 1: non-finite water height produced
-    int pad;
+    int ghostsAhead;         // 1: the current buffer's ghost ring already holds the next
+                             // step's boundary values (pushed by the update pass)
 };
 
 struct DomainDev {
     float *h[2], *hu[2], *hv[2];
     float *b;
     const BlockDesc *blocks;
-    const WorkUnit *units;
+    const WorkUnit *units;   // segments: block, rows [y0, y0+TY), columns [x0, x1)
+    const int *ctaSeg;       // CTA c owns segments [ctaSeg[c], ctaSeg[c+1])
     GroupState *groups;
     int nblocks;
     int solver, semantics, splitDtMode;

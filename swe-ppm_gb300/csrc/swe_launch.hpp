@@ -16,6 +16,14 @@ cudaError_t launchUpdateFH(const DomainDev &d, int nunits, int threads, cudaStre
 cudaError_t launchSpeedAug(const DomainDev &d, int nunits, int threads, cudaStream_t s);
 cudaError_t launchUpdateAug(const DomainDev &d, int nunits, int threads, cudaStream_t s);
 
+// resident CTAs per SM of the step kernels (the smaller of the two passes)
+int occupancyFH(int solver, int sem, int threads);
+int occupancyAug(int solver, int sem, int threads);
+inline int stepOccupancy(int solver, int sem, int threads) {
+    return (solver == SOLVER_FWAVE || solver == SOLVER_HLLE) ? occupancyFH(solver, sem, threads)
+                                                           : occupancyAug(solver, sem, threads);
+}
+
 inline cudaError_t launchSpeed(const DomainDev &d, int nunits, int threads, cudaStream_t s) {
     return (d.solver == SOLVER_FWAVE || d.solver == SOLVER_HLLE) ? launchSpeedFH(d, nunits, threads, s)
                                                                  : launchSpeedAug(d, nunits, threads, s);

@@ -1,27 +1,32 @@
 // Step kernels of the block step, templated on solver and semantics.
 //
-// One global time step of a group of blocks is three launches:
-//   ghostKernel      setGhostLayer: boundary conditions + on-device halo copies
-//                    between blocks (src/blocks/SWE_Block.hh:757-911,
-//                    src/blocks/SWE_DimensionalSplittingMPIOverdecomp.cpp:273-304)
+// One global time step of a group of blocks is two launches (plus a ghost
+// kernel only when the ghost ring is not already valid):
 //   sweepKernel<..., false>  speed pass: every edge's max wave speed, CTA max
-//                    by warp shuffles, group max by atomicMax; the last CTA of
-//                    the group turns it into maxTimestep
+//                    by warp shuffles, group max by atomicMax; the last
+//                    segment of the group turns it into maxTimestep
 //                    (src/blocks/SWE_DimensionalSplittingMpi.cpp:448-472)
 //   sweepKernel<..., true>   fused pass: solves every edge again, sums the net
 //                    updates per cell in registers and writes Q^{n+1} with the
 //                    dry clamp (src/blocks/SWE_DimensionalSplittingMpi.cpp:484-518)
-//                    or the split update (src/blocks/SWE_DimensionalSplitting.cpp:187-210)
+//                    or the split update (src/blocks/SWE_DimensionalSplitting.cpp:187-210),
+//                    then pushes the next step's ghost layer: boundary
+//                    conditions (src/blocks/SWE_Block.hh:757-911) and the copy
+//                    layers into the neighbour blocks' ghosts (the on-device
+//                    form of src/blocks/SWE_DimensionalSplittingMPIOverdecomp.cpp:273-304).
 // The speed pass is needed because dt depends on the same step's wave speeds;
 // at 2048^2 the state (67 MB) stays in L2 between the two passes, so DRAM
 // sees each input byte once.
 //
-// Tiling: a CTA owns TY = blockDim.x consecutive rows (one per thread, y is the
-// contiguous direction) of an x-chunk [x0, x1) of one block and marches along
-// x.  The x-edge (x-1|x) is solved from the previous column kept in registers;
-// the y-edge (y|y+1) from the neighbouring thread's cell in shared memory; the
-// tile's two boundary y-edges per column are solved up front.  Every cell's
-// update is finished one column later, when its right edge is known.
+// Work partition: the rows of every block are cut into tiles of TY rows and
+// the list of (tile, column) pairs of all blocks is split evenly over a
+// persistent grid (a few CTAs per SM); each CTA gets one or two contiguous
+// segments.  Within a segment a CTA owns TY consecutive rows (one per thread;
+// y is the contiguous direction) and marches along x.  The x-edge (x-1|x) is
+// solved from the previous column kept in registers, the y-edge (y|y+1) from
+// the neighbouring thread's cell in shared memory, and the tile's two boundary
+// y-edges per column are solved up front; a cell's update is finished one
+// column later, when its right edge is known.
 #pragma once
 
 #include "swe_device.cuh"
@@ -31,6 +36,7 @@ namespace swegb {
 __device__ __forceinline__ float blockReduceMax(float v, float *sRed) {
     for (int o = 16; o > 0; o >>= 1) v = vmax(v, __shfl_xor_sync(0xffffffffu, v, o));
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
     if (l == 0) sRed[w] = v;
     __syncthreads();
     if (w == 0) {
@@ -61,17 +67,143 @@ __device__ __forceinline__ bool groupActive(const GroupState *G) {
     return *((volatile const float *)&G->time) < *((volatile const float *)&G->target);
 }
 
+/// per-cell quantities in x (normal momentum hu) and y (hv) direction:
+/// u = hu * (1/h), v = hv * (1/h), sqrt(h), sqrt(g) sqrt(h)
 template <int S> __device__ __forceinline__ void cellQuantities(float h, float hu, float hv, float b, Cell &cx, Cell &cy) {
-    const bool wet = !(h < kDryTol);
     float sq = 0.f, c = 0.f, ux = 0.f, uy = 0.f;
     if (S != SOLVER_AUGRIE) {
+        const bool wet = !(h < kDryTol);
+        const float rh = 1.f / h;
         sq = sqrtf(h);
-        if (S == SOLVER_HLLE) c = sqrtf(kG * h);
-        ux = wet ? hu / h : 0.f;
-        uy = wet ? hv / h : 0.f;
+        if (S == SOLVER_HLLE) c = kSqrtG * sq;
+        ux = wet ? hu * rh : 0.f;
+        uy = wet ? hv * rh : 0.f;
     }
     cx = makeCell(h, hu, b, ux, sq, c);
     cy = makeCell(h, hv, b, uy, sq, c);
+}
+
+/// the segment's share of the running pass is done; the last segment of the
+/// group finishes the pass (dt after the speed pass; clock, step count and
+/// current buffer after the update pass)
+template <bool UPDATE>
+__device__ __forceinline__ void segmentDone(const DomainDev &d, GroupState *G, float segMax, float *sRed, int *sLast,
+                                            int cur) {
+    float m = 0.f;
+    if (!UPDATE) m = blockReduceMax(segMax, sRed);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (!UPDATE) atomicMax(&G->speedBits, __float_as_uint(m));
+        __threadfence();
+        const unsigned prev = atomicAdd(&G->arrived, 1u);
+        *sLast = (prev == unsigned(G->units) - 1u);
+    }
+    __syncthreads();
+    if (*sLast && threadIdx.x == 0) {
+        __threadfence();
+        if (UPDATE) {
+            G->arrived = 0u;
+            G->time = G->time + G->dt;
+            G->steps = G->steps + 1;
+            G->cur = cur ^ 1;
+            G->ghostsAhead = 1;
+        } else {
+            float s = __uint_as_float(atomicOr(&G->speedBits, 0u));
+            const BlockDesc &F = d.blocks[G->firstBlock];
+            if (d.semantics == SEM_SPLIT && d.splitDtMode == SPLIT_DT_LAST_EDGE) {
+                // speed of the last x-edge the serial loop solves: (nx | nx+1) in row ny+1
+                const float *Hc = pick(d.h, cur) + F.base, *HUc = pick(d.hu, cur) + F.base, *Bc = d.b + F.base;
+                const size_t o = size_t(F.nx) * size_t(F.pitch) + size_t(F.ny + 1);
+                const size_t o2 = o + size_t(F.pitch);
+                Cell L, R, dummy;
+                switch (d.solver) {
+                case SOLVER_FWAVE:
+                    cellQuantities<SOLVER_FWAVE>(Hc[o], HUc[o], 0.f, Bc[o], L, dummy);
+                    cellQuantities<SOLVER_FWAVE>(Hc[o2], HUc[o2], 0.f, Bc[o2], R, dummy);
+                    s = edgeSpeed<SOLVER_FWAVE>(L, R);
+                    break;
+                case SOLVER_HLLE:
+                    cellQuantities<SOLVER_HLLE>(Hc[o], HUc[o], 0.f, Bc[o], L, dummy);
+                    cellQuantities<SOLVER_HLLE>(Hc[o2], HUc[o2], 0.f, Bc[o2], R, dummy);
+                    s = edgeSpeed<SOLVER_HLLE>(L, R);
+                    break;
+                case SOLVER_AUGRIE:
+                    cellQuantities<SOLVER_AUGRIE>(Hc[o], HUc[o], 0.f, Bc[o], L, dummy);
+                    cellQuantities<SOLVER_AUGRIE>(Hc[o2], HUc[o2], 0.f, Bc[o2], R, dummy);
+                    s = edgeSpeed<SOLVER_AUGRIE>(L, R);
+                    break;
+                default:
+                    cellQuantities<SOLVER_HYBRID>(Hc[o], HUc[o], 0.f, Bc[o], L, dummy);
+                    cellQuantities<SOLVER_HYBRID>(Hc[o2], HUc[o2], 0.f, Bc[o2], R, dummy);
+                    s = edgeSpeed<SOLVER_HYBRID>(L, R);
+                    break;
+                }
+                s = vmax(0.f, s);
+            }
+            G->speed = s;
+            G->dt = timestepFromSpeed(s, F.dx, F.dy, d.semantics);
+            if (!(s == s)) G->status |= 1;  // NaN wave speed
+            G->speedBits = 0u;
+            G->arrived = 0u;
+        }
+        __threadfence();
+    }
+}
+
+/// pushes Q^{n+1} of a cell on the block's rim into every ghost cell whose
+/// value the next step's setGhostLayer takes from it (kept out of line: only
+/// rim cells call it)
+static __device__ __noinline__ void pushGhosts(const DomainDev &d, const BlockDesc &B, int outBuf, size_t P, int x,
+                                               int y, float h, float hu, float hv) {
+    float *HO = pick(d.h, outBuf), *HUO = pick(d.hu, outBuf), *HVO = pick(d.hv, outBuf);
+    const bool edgeX = (x == 1) || (x == B.nx);
+    const bool edgeY = (y == 1) || (y == B.ny);
+    // sides: LEFT (x == 1), RIGHT (x == nx), BOTTOM (y == 1), TOP (y == ny)
+    for (int side = 0; side < 4; side++) {
+        const bool on = side == 0 ? x == 1 : side == 1 ? x == B.nx : side == 2 ? y == 1 : y == B.ny;
+        if (!on) continue;
+        const int type = B.bnd[side];
+        const int gx = side == 0 ? 0 : side == 1 ? B.nx + 1 : x;
+        const int gy = side == 2 ? 0 : side == 3 ? B.ny + 1 : y;
+        const size_t g = size_t(B.base) + size_t(gx) * P + size_t(gy);
+        if (type == OUTFLOW) {
+            HO[g] = h; HUO[g] = hu; HVO[g] = hv;
+        } else if (type == WALL) {
+            HO[g] = h;
+            HUO[g] = side < 2 ? -hu : hu;
+            HVO[g] = side < 2 ? hv : -hv;
+        } else if (type == CONNECT_WITHIN_RANK) {
+            const BlockDesc &N = d.blocks[B.nbr[side]];
+            const int nxg = side == 0 ? N.nx + 1 : side == 1 ? 0 : x;
+            const int nyg = side == 2 ? N.ny + 1 : side == 3 ? 0 : y;
+            const size_t gn = size_t(N.base) + size_t(nxg) * size_t(N.pitch) + size_t(nyg);
+            HO[gn] = h; HUO[gn] = hu; HVO[gn] = hv;
+        } else {
+            // CONNECT, INFLOW, PASSIVE: the ghost keeps its value (set elsewhere)
+            const float *HI = pick(d.h, outBuf ^ 1), *HUI = pick(d.hu, outBuf ^ 1), *HVI = pick(d.hv, outBuf ^ 1);
+            HO[g] = HI[g]; HUO[g] = HUI[g]; HVO[g] = HVI[g];
+        }
+    }
+    // corners come from the diagonal interior cell whatever the boundary type
+    if (edgeX && edgeY) {
+        for (int cxi = 0; cxi < 2; cxi++)
+            for (int cyi = 0; cyi < 2; cyi++) {
+                const int sx = cxi ? B.nx : 1, sy = cyi ? B.ny : 1;
+                if (sx != x || sy != y) continue;
+                const size_t g = size_t(B.base) + size_t(cxi ? B.nx + 1 : 0) * P + size_t(cyi ? B.ny + 1 : 0);
+                HO[g] = h; HUO[g] = hu; HVO[g] = hv;
+            }
+    }
+}
+
+/// writes Q^{n+1} of cell (x, y); rim cells also refresh the ghost layer
+__device__ __forceinline__ void storeCell(const DomainDev &d, const BlockDesc &B, int outBuf, size_t P, int x, int y,
+                                          float h, float hu, float hv) {
+    const size_t o = size_t(B.base) + size_t(x) * P + size_t(y);
+    pick(d.h, outBuf)[o] = h;
+    pick(d.hu, outBuf)[o] = hu;
+    pick(d.hv, outBuf)[o] = hv;
+    if (x == 1 || x == B.nx || y == 1 || y == B.ny) pushGhosts(d, B, outBuf, P, x, y, h, hu, hv);
 }
 
 template <int S, int SEM, bool UPDATE>
@@ -83,226 +215,154 @@ __global__ void __launch_bounds__(kMaxTileRows) sweepKernel(const DomainDev d) {
     __shared__ float sRed[kMaxTileRows / 32];
     __shared__ int sLast;
 
-    const WorkUnit wu = d.units[blockIdx.x];
-    const BlockDesc B = d.blocks[wu.block];
-    GroupState *G = d.groups + B.group;
-    if (!groupActive(G)) return;
-    const int cur = G->cur;
-    const float *__restrict__ H = pick(d.h, cur) + B.base;
-    const float *__restrict__ HU = pick(d.hu, cur) + B.base;
-    const float *__restrict__ HV = pick(d.hv, cur) + B.base;
-    const float *__restrict__ BT = d.b + B.base;
-    const size_t P = size_t(B.pitch);
     const int t = threadIdx.x, TY = blockDim.x;
-    const int x0 = wu.x0, x1 = wu.x1, XC = x1 - x0;
-    const int y0 = wu.y0;
-    const int y = y0 + t;
-    const int yTop = min(y0 + TY - 1, B.ny);
-    const bool active = y <= yTop;
-    float smax = 0.f;
+    const int segEnd = d.ctaSeg[blockIdx.x + 1];
+    for (int seg = d.ctaSeg[blockIdx.x]; seg < segEnd; ++seg) {
+        const WorkUnit wu = d.units[seg];
+        const BlockDesc B = d.blocks[wu.block];
+        GroupState *G = d.groups + B.group;
+        if (!groupActive(G)) continue;
+        const int cur = G->cur;
+        const float *__restrict__ H = pick(d.h, cur) + B.base;
+        const float *__restrict__ HU = pick(d.hu, cur) + B.base;
+        const float *__restrict__ HV = pick(d.hv, cur) + B.base;
+        const float *__restrict__ BT = d.b + B.base;
+        const size_t P = size_t(B.pitch);
+        const int x0 = wu.x0, x1 = wu.x1, XC = x1 - x0;
+        const int y0 = wu.y0;
+        const int y = y0 + t;
+        const int yTop = min(y0 + TY - 1, B.ny);
+        const bool active = y <= yTop;
+        float smax = 0.f;
 
-    float dtdx = 0.f, dtdy = 0.f;
-    if (UPDATE) {
-        const float dt = G->dt;
-        dtdx = dt / B.dx;
-        dtdy = (SEM == SEM_SPLIT) ? dtdx : dt / B.dy;
-    }
-
-    // the tile's bottom (y0-1|y0) and top (yTop|yTop+1) y-edges of every column
-    for (int i = t; i < 2 * XC; i += TY) {
-        const bool top = i >= XC;
-        const int k = top ? i - XC : i;
-        const size_t o = size_t(x0 + k) * P + size_t(top ? yTop : y0 - 1);
-        Cell L, R, dummy;
-        cellQuantities<S>(H[o], HU[o], HV[o], BT[o], dummy, L);
-        cellQuantities<S>(H[o + 1], HU[o + 1], HV[o + 1], BT[o + 1], dummy, R);
+        float dtdx = 0.f, dtdy = 0.f;
         if (UPDATE) {
-            float aL, aR, auL, auR, s;
-            edgeSolve<S>(L, R, aL, aR, auL, auR, s);
-            if (top) {
-                sTop[0][k] = aL;
-                sTop[1][k] = auL;
-            } else {
-                sBot[0][k] = aR;
-                sBot[1][k] = auR;
-            }
-            // carry the ghost rows (set by this step's ghost layer) into the
-            // output buffer, where the reference keeps them after the update
-            const bool ghostRow = top ? (yTop == B.ny) : (y0 == 1);
-            if (ghostRow) {
-                const size_t g = top ? o + 1 : o;
-                pick(d.h, cur ^ 1)[B.base + g] = H[g];
-                pick(d.hu, cur ^ 1)[B.base + g] = HU[g];
-                pick(d.hv, cur ^ 1)[B.base + g] = HV[g];
-            }
-        } else {
-            smax = vmax(smax, edgeSpeed<S>(L, R));
-        }
-    }
-
-    float *__restrict__ HO = UPDATE ? pick(d.h, cur ^ 1) + B.base : nullptr;
-    float *__restrict__ HUO = UPDATE ? pick(d.hu, cur ^ 1) + B.base : nullptr;
-    float *__restrict__ HVO = UPDATE ? pick(d.hv, cur ^ 1) + B.base : nullptr;
-    if (UPDATE && t == 0) {  // corner ghosts of the block, carried over like the rest of the ring
-        const int cx[2] = {0, B.nx + 1}, cyy[2] = {0, B.ny + 1};
-        const bool hasX[2] = {x0 == 1, x1 == B.nx + 1}, hasY[2] = {y0 == 1, yTop == B.ny};
-        for (int i = 0; i < 2; i++)
-            for (int j = 0; j < 2; j++)
-                if (hasX[i] && hasY[j]) {
-                    const size_t o = size_t(cx[i]) * P + size_t(cyy[j]);
-                    HO[o] = H[o]; HUO[o] = HU[o]; HVO[o] = HV[o];
-                }
-    }
-
-    float nh = 0.f, nhu = 0.f, nhv = 0.f, nb = 0.f;
-    if (active) {
-        const size_t o = size_t(x0 - 1) * P + y;
-        nh = H[o]; nhu = HU[o]; nhv = HV[o]; nb = BT[o];
-    }
-    Cell prevX = makeCell(0.f, 0.f, 0.f, 0.f, 0.f, 0.f);
-    float pendH = 0.f, pendHU = 0.f;                 // right-going x-update into cell x
-    float oldH = 0.f, oldHU = 0.f, oldHV = 0.f;      // Q^n of cell x-1
-    float syH = 0.f, syHV = 0.f;                     // y net-update sums of cell x-1
-    bool bad = false;                                // a non-finite water height was produced
-
-    for (int x = x0 - 1; x <= x1; ++x) {
-        const float ch = nh, chu = nhu, chv = nhv, cb = nb;
-        if (x < x1 && active) {
-            const size_t o = size_t(x + 1) * P + y;
-            nh = H[o]; nhu = HU[o]; nhv = HV[o]; nb = BT[o];
-        }
-        Cell cx, cy;
-        cellQuantities<S>(ch, chu, chv, cb, cx, cy);
-        if (UPDATE && active && (x == 0 || x == B.nx + 1)) {  // ghost columns carried over
-            const size_t o = size_t(x) * P + y;
-            HO[o] = ch; HUO[o] = chu; HVO[o] = chv;
+            const float dt = G->dt;
+            dtdx = dt / B.dx;
+            dtdy = (SEM == SEM_SPLIT) ? dtdx : dt / B.dy;
         }
 
-        // x-edge (x-1 | x)
-        if (x >= x0 && active) {
+        __syncthreads();  // shared buffers of the previous segment are free
+        // the tile's bottom (y0-1|y0) and top (yTop|yTop+1) y-edges of every column
+        for (int i = t; i < 2 * XC; i += TY) {
+            const bool top = i >= XC;
+            const int k = top ? i - XC : i;
+            const size_t o = size_t(x0 + k) * P + size_t(top ? yTop : y0 - 1);
+            Cell L, R, dummy;
+            cellQuantities<S>(H[o], HU[o], HV[o], BT[o], dummy, L);
+            cellQuantities<S>(H[o + 1], HU[o + 1], HV[o + 1], BT[o + 1], dummy, R);
             if (UPDATE) {
                 float aL, aR, auL, auR, s;
-                edgeSolve<S>(prevX, cx, aL, aR, auL, auR, s);
-                if (x - 1 >= x0) {
-                    const size_t o = size_t(x - 1) * P + y;
-                    if (SEM == SEM_UNSPLIT) {
-                        const float sxH = pendH + aL, sxHU = pendHU + auL;
-                        float hn = oldH - (dtdx * sxH + dtdy * syH);
-                        float hun = oldHU - dtdx * sxHU;
-                        float hvn = oldHV - dtdy * syHV;
-                        if (hn < 0.f) {
-                            hn = 0.f; hun = 0.f; hvn = 0.f;
-                        } else if (hn < 0.1f) {
-                            hun = 0.f; hvn = 0.f;
+                edgeSolve<S>(L, R, aL, aR, auL, auR, s);
+                if (top) {
+                    sTop[0][k] = aL;
+                    sTop[1][k] = auL;
+                } else {
+                    sBot[0][k] = aR;
+                    sBot[1][k] = auR;
+                }
+            } else {
+                smax = vmax(smax, edgeSpeed<S>(L, R));
+            }
+        }
+
+        float nh = 0.f, nhu = 0.f, nhv = 0.f, nb = 0.f;
+        if (active) {
+            const size_t o = size_t(x0 - 1) * P + y;
+            nh = H[o]; nhu = HU[o]; nhv = HV[o]; nb = BT[o];
+        }
+        Cell prevX = makeCell(0.f, 0.f, 0.f, 0.f, 0.f, 0.f);
+        float pendH = 0.f, pendHU = 0.f;             // right-going x-update into cell x
+        float oldH = 0.f, oldHU = 0.f, oldHV = 0.f;  // Q^n of cell x-1
+        float syH = 0.f, syHV = 0.f;                 // y net-update sums of cell x-1
+        bool bad = false;                            // a non-finite water height was produced
+
+        for (int x = x0 - 1; x <= x1; ++x) {
+            const float ch = nh, chu = nhu, chv = nhv, cb = nb;
+            if (x < x1 && active) {
+                const size_t o = size_t(x + 1) * P + y;
+                nh = H[o]; nhu = HU[o]; nhv = HV[o]; nb = BT[o];
+            }
+            Cell cx, cy;
+            cellQuantities<S>(ch, chu, chv, cb, cx, cy);
+
+            // x-edge (x-1 | x)
+            if (x >= x0 && active) {
+                if (UPDATE) {
+                    float aL, aR, auL, auR, s;
+                    edgeSolve<S>(prevX, cx, aL, aR, auL, auR, s);
+                    if (x - 1 >= x0) {
+                        float hn, hun, hvn;
+                        if (SEM == SEM_UNSPLIT) {
+                            const float sxH = pendH + aL, sxHU = pendHU + auL;
+                            hn = oldH - (dtdx * sxH + dtdy * syH);
+                            hun = oldHU - dtdx * sxHU;
+                            hvn = oldHV - dtdy * syHV;
+                            if (hn < 0.f) {
+                                hn = 0.f; hun = 0.f; hvn = 0.f;
+                            } else if (hn < 0.1f) {
+                                hun = 0.f; hvn = 0.f;
+                            }
+                        } else {
+                            const float sxH = aL + pendH, sxHU = auL + pendHU;
+                            const float hStar = oldH - dtdx * sxH;
+                            hn = hStar - dtdx * syH;
+                            hun = oldHU - dtdx * sxHU;
+                            hvn = oldHV - dtdx * syHV;
                         }
                         bad |= !(fabsf(hn) <= FLT_MAX);
-                        HO[o] = hn; HUO[o] = hun; HVO[o] = hvn;
-                    } else {
-                        const float sxH = aL + pendH, sxHU = auL + pendHU;
-                        const float hStar = oldH - dtdx * sxH;
-                        const float hn = hStar - dtdx * syH;
-                        bad |= !(fabsf(hn) <= FLT_MAX);
-                        HO[o] = hn;
-                        HUO[o] = oldHU - dtdx * sxHU;
-                        HVO[o] = oldHV - dtdx * syHV;
+                        storeCell(d, B, cur ^ 1, P, x - 1, y, hn, hun, hvn);
                     }
-                }
-                pendH = aR;
-                pendHU = auR;
-            } else {
-                smax = vmax(smax, edgeSpeed<S>(prevX, cx));
-            }
-        }
-        prevX = cx;
-
-        // y-edges of column x
-        if (x >= x0 && x < x1) {
-            const int buf = x & 1;
-            sC[buf][0][t] = cy.h; sC[buf][1][t] = cy.hn; sC[buf][2][t] = cy.b;
-            sC[buf][3][t] = cy.u; sC[buf][4][t] = cy.sq; sC[buf][5][t] = cy.c;
-            __syncthreads();
-            float bLh = 0.f, bLhv = 0.f;
-            if (active && y < yTop) {
-                const Cell up = makeCell(sC[buf][0][t + 1], sC[buf][1][t + 1], sC[buf][2][t + 1],
-                                         sC[buf][3][t + 1], sC[buf][4][t + 1], sC[buf][5][t + 1]);
-                if (UPDATE) {
-                    float bR, bRhv, s;
-                    edgeSolve<S>(cy, up, bLh, bR, bLhv, bRhv, s);
-                    sR[buf][0][t + 1] = bR;
-                    sR[buf][1][t + 1] = bRhv;
+                    pendH = aR;
+                    pendHU = auR;
                 } else {
-                    smax = vmax(smax, edgeSpeed<S>(cy, up));
+                    smax = vmax(smax, edgeSpeed<S>(prevX, cx));
                 }
             }
-            if (UPDATE) {
-                __syncthreads();
-                if (active) {
-                    if (y == yTop) {
-                        bLh = sTop[0][x - x0];
-                        bLhv = sTop[1][x - x0];
-                    }
-                    const float rH = (t == 0) ? sBot[0][x - x0] : sR[buf][0][t];
-                    const float rHV = (t == 0) ? sBot[1][x - x0] : sR[buf][1][t];
-                    if (SEM == SEM_UNSPLIT) {
-                        syH = rH + bLh;
-                        syHV = rHV + bLhv;
-                    } else {
-                        syH = bLh + rH;
-                        syHV = bLhv + rHV;
-                    }
-                    oldH = ch; oldHU = chu; oldHV = chv;
-                }
-            }
-        }
-    }
+            prevX = cx;
 
-    if (UPDATE) {
-        // the last CTA of the group advances the group's clock and buffer
-        if (__syncthreads_or(bad) && t == 0) atomicOr(&G->status, 2);
-        if (t == 0) {
-            __threadfence();
-            const unsigned prev = atomicAdd(&G->arrived, 1u);
-            sLast = (prev == unsigned(G->units) - 1u);
-        }
-        __syncthreads();
-        if (sLast && t == 0) {
-            __threadfence();
-            G->arrived = 0u;
-            G->time = G->time + G->dt;
-            G->steps = G->steps + 1;
-            G->cur = cur ^ 1;
-            __threadfence();
-        }
-    } else {
-        const float m = blockReduceMax(smax, sRed);
-        if (t == 0) {
-            atomicMax(&G->speedBits, __float_as_uint(m));
-            __threadfence();
-            const unsigned prev = atomicAdd(&G->arrived, 1u);
-            sLast = (prev == unsigned(G->units) - 1u);
-        }
-        __syncthreads();
-        if (sLast && t == 0) {
-            __threadfence();
-            float s = __uint_as_float(atomicOr(&G->speedBits, 0u));
-            const BlockDesc &F = d.blocks[G->firstBlock];
-            if (SEM == SEM_SPLIT && d.splitDtMode == SPLIT_DT_LAST_EDGE) {
-                // speed of the last x-edge the serial loop solves: (nx | nx+1) in row ny+1
-                const float *Hc = pick(d.h, cur) + F.base, *HUc = pick(d.hu, cur) + F.base, *Bc = d.b + F.base;
-                const size_t o = size_t(F.nx) * size_t(F.pitch) + size_t(F.ny + 1);
-                const size_t o2 = o + size_t(F.pitch);
-                Cell L, R, dummy;
-                cellQuantities<S>(Hc[o], HUc[o], 0.f, Bc[o], L, dummy);
-                cellQuantities<S>(Hc[o2], HUc[o2], 0.f, Bc[o2], R, dummy);
-                s = vmax(0.f, edgeSpeed<S>(L, R));
+            // y-edges of column x
+            if (x >= x0 && x < x1) {
+                const int buf = x & 1;
+                sC[buf][0][t] = cy.h; sC[buf][1][t] = cy.hn; sC[buf][2][t] = cy.b;
+                sC[buf][3][t] = cy.u; sC[buf][4][t] = cy.sq; sC[buf][5][t] = cy.c;
+                __syncthreads();
+                float bLh = 0.f, bLhv = 0.f;
+                if (active && y < yTop) {
+                    const Cell up = makeCell(sC[buf][0][t + 1], sC[buf][1][t + 1], sC[buf][2][t + 1],
+                                             sC[buf][3][t + 1], sC[buf][4][t + 1], sC[buf][5][t + 1]);
+                    if (UPDATE) {
+                        float bR, bRhv, s;
+                        edgeSolve<S>(cy, up, bLh, bR, bLhv, bRhv, s);
+                        sR[buf][0][t + 1] = bR;
+                        sR[buf][1][t + 1] = bRhv;
+                    } else {
+                        smax = vmax(smax, edgeSpeed<S>(cy, up));
+                    }
+                }
+                if (UPDATE) {
+                    __syncthreads();
+                    if (active) {
+                        if (y == yTop) {
+                            bLh = sTop[0][x - x0];
+                            bLhv = sTop[1][x - x0];
+                        }
+                        const float rH = (t == 0) ? sBot[0][x - x0] : sR[buf][0][t];
+                        const float rHV = (t == 0) ? sBot[1][x - x0] : sR[buf][1][t];
+                        if (SEM == SEM_UNSPLIT) {
+                            syH = rH + bLh;
+                            syHV = rHV + bLhv;
+                        } else {
+                            syH = bLh + rH;
+                            syHV = bLhv + rHV;
+                        }
+                        oldH = ch; oldHU = chu; oldHV = chv;
+                    }
+                }
             }
-            G->speed = s;
-            G->dt = timestepFromSpeed(s, F.dx, F.dy, SEM);
-            if (!(s == s)) G->status |= 1;  // NaN wave speed
-            G->speedBits = 0u;
-            G->arrived = 0u;
-            __threadfence();
         }
+        if (UPDATE && __syncthreads_or(bad) && t == 0) atomicOr(&G->status, 2);
+        segmentDone<UPDATE>(d, G, smax, sRed, &sLast, cur);
     }
 }
 
@@ -311,61 +371,37 @@ __global__ void __launch_bounds__(kMaxTileRows) sweepKernel(const DomainDev d) {
 template <int S> __global__ void __launch_bounds__(kMaxTileRows) speedSplitKernel(const DomainDev d) {
     __shared__ float sRed[kMaxTileRows / 32];
     __shared__ int sLast;
-    const WorkUnit wu = d.units[blockIdx.x];
-    const BlockDesc B = d.blocks[wu.block];
-    GroupState *G = d.groups + B.group;
-    if (!groupActive(G)) return;
-    const int cur = G->cur;
-    const float *__restrict__ H = pick(d.h, cur) + B.base;
-    const float *__restrict__ HU = pick(d.hu, cur) + B.base;
-    const float *__restrict__ BT = d.b + B.base;
-    const size_t P = size_t(B.pitch);
     const int TY = blockDim.x;
-    const int yTop = min(wu.y0 + TY - 1, B.ny);
-    const int rLo = (wu.y0 == 1) ? 0 : wu.y0;
-    const int rHi = (yTop == B.ny) ? B.ny + 1 : yTop;
-    float smax = 0.f;
-    for (int r = rLo + int(threadIdx.x); r <= rHi; r += TY) {
-        Cell prev, dummy;
-        {
-            const size_t o = size_t(wu.x0 - 1) * P + r;
-            cellQuantities<S>(H[o], HU[o], 0.f, BT[o], prev, dummy);
+    const int segEnd = d.ctaSeg[blockIdx.x + 1];
+    for (int seg = d.ctaSeg[blockIdx.x]; seg < segEnd; ++seg) {
+        const WorkUnit wu = d.units[seg];
+        const BlockDesc B = d.blocks[wu.block];
+        GroupState *G = d.groups + B.group;
+        if (!groupActive(G)) continue;
+        const int cur = G->cur;
+        const float *__restrict__ H = pick(d.h, cur) + B.base;
+        const float *__restrict__ HU = pick(d.hu, cur) + B.base;
+        const float *__restrict__ BT = d.b + B.base;
+        const size_t P = size_t(B.pitch);
+        const int yTop = min(wu.y0 + TY - 1, B.ny);
+        const int rLo = (wu.y0 == 1) ? 0 : wu.y0;
+        const int rHi = (yTop == B.ny) ? B.ny + 1 : yTop;
+        float smax = 0.f;
+        for (int r = rLo + int(threadIdx.x); r <= rHi; r += TY) {
+            Cell prev, dummy;
+            {
+                const size_t o = size_t(wu.x0 - 1) * P + r;
+                cellQuantities<S>(H[o], HU[o], 0.f, BT[o], prev, dummy);
+            }
+            for (int x = wu.x0; x <= wu.x1; ++x) {
+                const size_t o = size_t(x) * P + r;
+                Cell c;
+                cellQuantities<S>(H[o], HU[o], 0.f, BT[o], c, dummy);
+                smax = vmax(smax, edgeSpeed<S>(prev, c));
+                prev = c;
+            }
         }
-        for (int x = wu.x0; x <= wu.x1; ++x) {
-            const size_t o = size_t(x) * P + r;
-            Cell c;
-            cellQuantities<S>(H[o], HU[o], 0.f, BT[o], c, dummy);
-            smax = vmax(smax, edgeSpeed<S>(prev, c));
-            prev = c;
-        }
-    }
-    const float m = blockReduceMax(smax, sRed);
-    if (threadIdx.x == 0) {
-        atomicMax(&G->speedBits, __float_as_uint(m));
-        __threadfence();
-        const unsigned prev = atomicAdd(&G->arrived, 1u);
-        sLast = (prev == unsigned(G->units) - 1u);
-    }
-    __syncthreads();
-    if (sLast && threadIdx.x == 0) {
-        __threadfence();
-        float s = __uint_as_float(atomicOr(&G->speedBits, 0u));
-        const BlockDesc &F = d.blocks[G->firstBlock];
-        if (d.splitDtMode == SPLIT_DT_LAST_EDGE) {
-            const float *Hc = pick(d.h, cur) + F.base, *HUc = pick(d.hu, cur) + F.base, *Bc = d.b + F.base;
-            const size_t o = size_t(F.nx) * size_t(F.pitch) + size_t(F.ny + 1);
-            const size_t o2 = o + size_t(F.pitch);
-            Cell L, R, dummy;
-            cellQuantities<S>(Hc[o], HUc[o], 0.f, Bc[o], L, dummy);
-            cellQuantities<S>(Hc[o2], HUc[o2], 0.f, Bc[o2], R, dummy);
-            s = vmax(0.f, edgeSpeed<S>(L, R));
-        }
-        G->speed = s;
-        G->dt = timestepFromSpeed(s, F.dx, F.dy, SEM_SPLIT);
-        if (!(s == s)) G->status |= 1;
-        G->speedBits = 0u;
-        G->arrived = 0u;
-        __threadfence();
+        segmentDone<false>(d, G, smax, sRed, &sLast, cur);
     }
 }
 
