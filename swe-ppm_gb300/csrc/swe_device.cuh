@@ -120,9 +120,7 @@ __device__ __forceinline__ void routeWave(float s, float zh, float zhu, float &h
 
 // wet/dry pre-step of the f-wave and HLLE solvers: a dry side becomes the
 // reflection of the wet side (a wall).  Returns false for a dry/dry edge.
-__device__ __forceinline__ bool reflectDry(Cell &L, Cell &R, bool &dryL, bool &dryR) {
-    dryL = L.h < kDryTol;
-    dryR = R.h < kDryTol;
+__device__ __forceinline__ bool reflectDry(Cell &L, Cell &R, bool dryL, bool dryR) {
     if (dryL && dryR) return false;
     if (dryL) {
         L.h = R.h; L.hn = -R.hn; L.u = -R.u; L.sq = R.sq; L.c = R.c; L.b = R.b;
@@ -132,6 +130,9 @@ __device__ __forceinline__ bool reflectDry(Cell &L, Cell &R, bool &dryL, bool &d
     return true;
 }
 
+/// wave speeds; fminf/fmaxf equal the (b < a ? b : a) selection of the CPU
+/// restatement for every non-NaN input up to the sign of a zero, which no
+/// later operation can observe
 template <int S>
 __device__ __forceinline__ void waveSpeeds(const Cell &L, const Cell &R, float &s1, float &s2) {
     const float uRoe = fmaf(L.u, L.sq, R.u * R.sq) / (L.sq + R.sq);
@@ -140,20 +141,31 @@ __device__ __forceinline__ void waveSpeeds(const Cell &L, const Cell &R, float &
         s1 = uRoe - cRoe;
         s2 = uRoe + cRoe;
     } else {
-        s1 = vmin(L.u - L.c, uRoe - cRoe);
-        s2 = vmax(R.u + R.c, uRoe + cRoe);
+        s1 = fminf(L.u - L.c, uRoe - cRoe);
+        s2 = fmaxf(R.u + R.c, uRoe + cRoe);
     }
 }
 
-/// f-wave (S = SOLVER_FWAVE) or HLLE (S = SOLVER_HLLE) net updates of one edge.
+/// share of a wave with speed s that goes to the left cell: 1, 0 or 1/2
+/// (|s| <= zeroTol); the right cell gets 1 minus that.  Products with these
+/// weights are exact, so weighting equals the branchy routing bit for bit.
+__device__ __forceinline__ float leftShare(float s) {
+    return (s < -kZeroTol) ? 1.f : ((s > kZeroTol) ? 0.f : 0.5f);
+}
+
+/// f-wave (S = SOLVER_FWAVE) or HLLE (S = SOLVER_HLLE) net updates of one
+/// edge.  Wet/wet edges run straight through; an edge with a dry side takes
+/// the (warp-uniform away from shorelines) reflection branch.
 template <int S>
 __device__ __forceinline__ void edgeFH(Cell L, Cell R, float &hUpdL, float &hUpdR, float &huUpdL, float &huUpdR,
                                        float &speed) {
-    hUpdL = 0.f; hUpdR = 0.f; huUpdL = 0.f; huUpdR = 0.f;
-    bool dryL, dryR;
-    if (!reflectDry(L, R, dryL, dryR)) {
-        speed = 0.f;
-        return;
+    const bool dryL = L.h < kDryTol, dryR = R.h < kDryTol;
+    if (dryL || dryR) {
+        if (!reflectDry(L, R, dryL, dryR)) {
+            hUpdL = 0.f; hUpdR = 0.f; huUpdL = 0.f; huUpdR = 0.f;
+            speed = 0.f;
+            return;
+        }
     }
     float s1, s2;
     waveSpeeds<S>(L, R, s1, s2);
@@ -164,20 +176,26 @@ __device__ __forceinline__ void edgeFH(Cell L, Cell R, float &hUpdL, float &hUpd
     const float rd = 1.f / (s2 - s1);
     const float beta1 = fmaf(s2, df1, -df2) * rd;
     const float beta2 = fmaf(-s1, df1, df2) * rd;
-    routeWave(s1, beta1, beta1 * s1, hUpdL, hUpdR, huUpdL, huUpdR);
-    routeWave(s2, beta2, beta2 * s2, hUpdL, hUpdR, huUpdL, huUpdR);
+    const float w1 = leftShare(s1), w2 = leftShare(s2);
+    const float z1u = beta1 * s1, z2u = beta2 * s2;
+    hUpdL = fmaf(w2, beta2, w1 * beta1);
+    hUpdR = fmaf(1.f - w2, beta2, (1.f - w1) * beta1);
+    huUpdL = fmaf(w2, z2u, w1 * z1u);
+    huUpdR = fmaf(1.f - w2, z2u, (1.f - w1) * z1u);
     if (dryL) { hUpdL = 0.f; huUpdL = 0.f; }
     if (dryR) { hUpdR = 0.f; huUpdR = 0.f; }
-    speed = vmax(fabsf(s1), fabsf(s2));
+    speed = fmaxf(fabsf(s1), fabsf(s2));
 }
 
 /// max wave speed of one edge, bit-identical to edgeFH's `speed`
 template <int S> __device__ __forceinline__ float edgeSpeedFH(Cell L, Cell R) {
-    bool dryL, dryR;
-    if (!reflectDry(L, R, dryL, dryR)) return 0.f;
+    const bool dryL = L.h < kDryTol, dryR = R.h < kDryTol;
+    if (dryL || dryR) {
+        if (!reflectDry(L, R, dryL, dryR)) return 0.f;
+    }
     float s1, s2;
     waveSpeeds<S>(L, R, s1, s2);
-    return vmax(fabsf(s1), fabsf(s2));
+    return fmaxf(fabsf(s1), fabsf(s2));
 }
 
 // ---------------------------------------------------------------------------
