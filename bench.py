@@ -123,8 +123,9 @@ def setup_domain(swe, device, n=N_CELLS_SIDE):
     geo, h, hu, hv, b = swe.init_domain(swe.SCENARIO_TSUNAMI, n, n, N_BLOCKS, [n, SEED, 100000.0])
     tile_rows = int(os.environ.get("SWE_TILE_ROWS", "0"))
     tile_cols = int(os.environ.get("SWE_TILE_COLS", "0"))
+    variant = int(os.environ.get("SWE_KERNEL_VARIANT", "0"))
     D = swe.Domain(geo["nx_cols"], geo["ny_rows"], geo["dx"], geo["dy"], boundary=geo["boundary"], solver=swe.HLLE,
-                   tile_rows=tile_rows, tile_cols=tile_cols, device=device)
+                   tile_rows=tile_rows, tile_cols=tile_cols, device=device, kernel_variant=variant)
     D.upload(h, hu, hv, b)
     D.exchange_bathymetry()
     return D, geo, (h, hu, hv, b)

@@ -83,8 +83,11 @@ typedef struct swe_gpu_desc {
     int semantics;       /* SWE_SEMANTICS_* */
     int split_dt_mode;   /* SWE_SPLIT_DT_* (split semantics only) */
     int tile_rows;       /* rows per CTA (multiple of 32, <= 256); 0 = default */
-    int tile_cols;       /* columns per x-chunk (<= 128); 0 = default */
+    int tile_cols;       /* max columns per work segment (<= 128 for the tile mapping); 0 = default */
     int device;          /* CUDA device ordinal */
+    int kernel_variant;  /* thread mapping of the sweep kernels: 0 = CTA tiles of
+                            tile_rows rows (default), 1 / 2 / 3 = warp strips of
+                            4 / 2 / 1 rows per lane */
 } swe_gpu_desc;
 
 int swe_gpu_domain_create(const swe_gpu_desc *desc, swe_gpu_domain **out);

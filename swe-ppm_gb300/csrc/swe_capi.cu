@@ -15,6 +15,7 @@
 #include "swe_device.cuh"
 #include "swe_launch.hpp"
 
+
 using namespace swegb;
 
 namespace {
@@ -179,6 +180,7 @@ struct swe_gpu_domain {
     cudaStream_t stream = nullptr;     // stream launches go to
     cudaStream_t ownStream = nullptr;  // the handle's own stream
     int solver = SOLVER_HLLE, semantics = SEM_UNSPLIT, splitDtMode = SPLIT_DT_MAX;
+    int variant = VARIANT_WARP;
     int tileRows = 256, tileCols = 32;
     std::vector<BlockDesc> blocks;
     std::vector<WorkUnit> units;
@@ -191,8 +193,13 @@ struct swe_gpu_domain {
     WorkUnit *dUnits = nullptr;
     int *dCtaSeg = nullptr;
     GroupState *dGroups = nullptr;
-    std::vector<int> ctaSeg;      // CTA c owns segments [ctaSeg[c], ctaSeg[c+1])
-    int grid = 0;                 // CTAs of the sweep kernels
+    std::vector<int> ctaSeg;      // speed pass: worker c owns segments [ctaSeg[c], ctaSeg[c+1])
+    int grid = 0;                 // CTAs of the speed pass
+    std::vector<WorkUnit> unitsU; // update pass segments and owners
+    std::vector<int> ctaSegU;
+    int gridU = 0;
+    WorkUnit *dUnitsU = nullptr;
+    int *dCtaSegU = nullptr;
     bool ghostsValid = false;     // the current buffer's ghost ring matches its interior
     DomainDev dev{};
     float *stage = nullptr;       // host-order staging for transfers (4 fields)
@@ -213,12 +220,18 @@ int enqueueGhost(swe_gpu_domain *D, int bathymetry) {
 }
 
 int enqueueSpeed(swe_gpu_domain *D) {
-    CUDA_TRY(launchSpeed(D->dev, D->grid, D->tileRows, D->stream));
+    DomainDev d = D->dev;
+    d.units = D->dUnits;
+    d.ctaSeg = D->dCtaSeg;
+    CUDA_TRY(launchSpeed(d, D->grid, D->tileRows, D->stream));
     return SWE_GPU_OK;
 }
 
 int enqueueUpdate(swe_gpu_domain *D) {
-    CUDA_TRY(launchUpdate(D->dev, D->grid, D->tileRows, D->stream));
+    DomainDev d = D->dev;
+    d.units = D->dUnitsU;
+    d.ctaSeg = D->dCtaSegU;
+    CUDA_TRY(launchUpdate(d, D->gridU, D->tileRows, D->stream));
     D->ghostsValid = true;  // the update pass pushed the next ghost ring
     return SWE_GPU_OK;
 }
@@ -262,6 +275,8 @@ void freeDomain(swe_gpu_domain *D) {
     cudaFree(D->dBlocks);
     cudaFree(D->dUnits);
     cudaFree(D->dCtaSeg);
+    cudaFree(D->dUnitsU);
+    cudaFree(D->dCtaSegU);
     cudaFree(D->dGroups);
     if (D->ownStream) cudaStreamDestroy(D->ownStream);
     delete D;
@@ -312,6 +327,10 @@ int swe_gpu_domain_create(const swe_gpu_desc *desc, swe_gpu_domain **out) {
     D->solver = desc->solver;
     D->semantics = desc->semantics;
     D->splitDtMode = desc->split_dt_mode;
+    D->variant = desc->kernel_variant == 1   ? VARIANT_WARP
+                 : desc->kernel_variant == 2 ? VARIANT_WARP2
+                 : desc->kernel_variant == 3 ? VARIANT_WARP1
+                                             : VARIANT_TILE;
     int maxNy = 0;
     for (int i = 0; i < by; i++) maxNy = std::max(maxNy, desc->ny_rows[i]);
     D->tileRows = std::min(tileRows, ((maxNy + 31) / 32) * 32);
@@ -356,30 +375,41 @@ int swe_gpu_domain_create(const swe_gpu_desc *desc, swe_gpu_domain **out) {
     }
     elems += 32;  // slack so the last column's padding stays inside the allocation
     D->fieldElems = elems;
-    // Balanced persistent partition: the (row tile, column) pairs of all blocks
-    // in order, split into `grid` equal runs; a run that crosses a tile or a
-    // block boundary becomes several segments.  tile_cols, when given, caps
-    // the segment length.
-    {
+    // Balanced persistent partitions, one per pass (the two kernels differ in
+    // registers and therefore in resident CTAs): the (row tile, column) pairs
+    // of all blocks in order, split into `workers` equal runs (a worker is a
+    // CTA for the tile mapping, a warp for the warp mappings); a run that
+    // crosses a tile or a block boundary becomes several segments.  tile_cols,
+    // when given, caps the segment length and raises the number of workers.
+    for (int pass = 0; pass < 2; pass++) {
         int sms = 148;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, D->device);
-        const int perSM = std::max(1, std::min(16, stepOccupancy(D->solver, D->semantics, D->tileRows)));
+        const bool warp = D->variant != VARIANT_TILE;
+        const int rows = D->variant == VARIANT_WARP ? 4 : D->variant == VARIANT_WARP2 ? 2 : 1;
+        const int rowsPerTile = warp ? 32 * rows : D->tileRows;
+        const int occ = passOccupancy(D->variant, D->solver, D->semantics, pass == 1, D->tileRows);
+        const long long perSM = warp ? std::max(1, std::min(64, 4 * occ)) : std::max(1, std::min(16, occ));
         long long total = 0;
-        for (const BlockDesc &B : D->blocks) total += (long long)((B.ny + D->tileRows - 1) / D->tileRows) * B.nx;
-        const long long want = desc->tile_cols > 0 ? (total + desc->tile_cols - 1) / desc->tile_cols : (long long)sms * perSM;
-        D->grid = int(std::max(1LL, std::min(total, std::max(want, (long long)sms * perSM))));
-        D->ctaSeg.assign(1, 0);
+        for (const BlockDesc &B : D->blocks) total += (long long)((B.ny + rowsPerTile - 1) / rowsPerTile) * B.nx;
+        long long workers = (long long)sms * perSM;
+        if (desc->tile_cols > 0) workers = std::max(workers, (total + desc->tile_cols - 1) / desc->tile_cols);
+        workers = std::max(1LL, std::min(total, workers));
+        if (warp) workers = (workers + 3) / 4 * 4;  // whole CTAs of 4 warps
+        std::vector<WorkUnit> &units = pass ? D->unitsU : D->units;
+        std::vector<int> &ctaSeg = pass ? D->ctaSegU : D->ctaSeg;
+        (pass ? D->gridU : D->grid) = int(warp ? workers / 4 : workers);
+        ctaSeg.assign(1, 0);
         long long pos = 0;  // global (tile, column) index
         int k = 0, tile = 0, col = 1;
-        auto tiles = [&](int kk) { return (D->blocks[kk].ny + D->tileRows - 1) / D->tileRows; };
-        for (int c = 0; c < D->grid; c++) {
-            long long end = total * (c + 1) / D->grid;
+        auto tiles = [&](int kk) { return (D->blocks[kk].ny + rowsPerTile - 1) / rowsPerTile; };
+        for (long long c = 0; c < workers; c++) {
+            const long long end = total * (c + 1) / workers;
             while (pos < end) {
                 const BlockDesc &B = D->blocks[k];
                 const long long take = std::min<long long>(end - pos, (long long)(B.nx + 1 - col));
-                const int cap = desc->tile_cols > 0 ? desc->tile_cols : kMaxTileCols;
+                const int cap = desc->tile_cols > 0 ? desc->tile_cols : (warp ? (1 << 30) : kMaxTileCols);
                 const int len = int(std::min<long long>(take, cap));
-                D->units.push_back(WorkUnit{k, 1 + tile * D->tileRows, col, col + len});
+                units.push_back(WorkUnit{k, 1 + tile * rowsPerTile, col, col + len});
                 pos += len;
                 col += len;
                 if (col > B.nx) {
@@ -390,11 +420,12 @@ int swe_gpu_domain_create(const swe_gpu_desc *desc, swe_gpu_domain **out) {
                     }
                 }
             }
-            D->ctaSeg.push_back(int(D->units.size()));
+            ctaSeg.push_back(int(units.size()));
         }
     }
     GroupState g0{};
     g0.units = int(D->units.size());
+    g0.unitsUpd = int(D->unitsU.size());
     g0.firstBlock = 0;
     g0.target = INFINITY;
     g0.dt = 0.f;
@@ -411,6 +442,8 @@ int swe_gpu_domain_create(const swe_gpu_desc *desc, swe_gpu_domain **out) {
     ok = ok && cudaMalloc(&D->dBlocks, sizeof(BlockDesc) * D->blocks.size()) == cudaSuccess;
     ok = ok && cudaMalloc(&D->dUnits, sizeof(WorkUnit) * D->units.size()) == cudaSuccess;
     ok = ok && cudaMalloc(&D->dCtaSeg, sizeof(int) * D->ctaSeg.size()) == cudaSuccess;
+    ok = ok && cudaMalloc(&D->dUnitsU, sizeof(WorkUnit) * D->unitsU.size()) == cudaSuccess;
+    ok = ok && cudaMalloc(&D->dCtaSegU, sizeof(int) * D->ctaSegU.size()) == cudaSuccess;
     ok = ok && cudaMalloc(&D->dGroups, sizeof(GroupState) * D->ngroups) == cudaSuccess;
     if (!ok) {
         cudaGetLastError();
@@ -426,6 +459,8 @@ int swe_gpu_domain_create(const swe_gpu_desc *desc, swe_gpu_domain **out) {
     cudaMemcpyAsync(D->dBlocks, D->blocks.data(), sizeof(BlockDesc) * D->blocks.size(), cudaMemcpyHostToDevice, D->stream);
     cudaMemcpyAsync(D->dUnits, D->units.data(), sizeof(WorkUnit) * D->units.size(), cudaMemcpyHostToDevice, D->stream);
     cudaMemcpyAsync(D->dCtaSeg, D->ctaSeg.data(), sizeof(int) * D->ctaSeg.size(), cudaMemcpyHostToDevice, D->stream);
+    cudaMemcpyAsync(D->dUnitsU, D->unitsU.data(), sizeof(WorkUnit) * D->unitsU.size(), cudaMemcpyHostToDevice, D->stream);
+    cudaMemcpyAsync(D->dCtaSegU, D->ctaSegU.data(), sizeof(int) * D->ctaSegU.size(), cudaMemcpyHostToDevice, D->stream);
     cudaMemcpyAsync(D->dGroups, D->groupsInit.data(), sizeof(GroupState) * D->ngroups, cudaMemcpyHostToDevice, D->stream);
     e = cudaStreamSynchronize(D->stream);
     if (e != cudaSuccess) {
@@ -446,6 +481,7 @@ int swe_gpu_domain_create(const swe_gpu_desc *desc, swe_gpu_domain **out) {
     D->dev.solver = D->solver;
     D->dev.semantics = D->semantics;
     D->dev.splitDtMode = D->splitDtMode;
+    D->dev.variant = D->variant;
     *out = D;
     return SWE_GPU_OK;
 }
@@ -779,6 +815,7 @@ __global__ void noallocSetupKernel(NoAllocScratch *s, BlockDesc b, int tileRows,
         g.speedBits = 0u;
         g.arrived = 0u;
         g.units = nunits;
+        g.unitsUpd = nunits;
         g.firstBlock = 0;
         g.dt = 0.f;
         g.speed = 0.f;
@@ -856,6 +893,7 @@ extern "C" int swe_gpu_step_block_noalloc(int solver, int semantics, int nx, int
     d.solver = solver;
     d.semantics = semantics;
     d.splitDtMode = SPLIT_DT_MAX;
+    d.variant = VARIANT_TILE;  // one work unit per CTA, built by the set-up kernel
     cudaStream_t s = static_cast<cudaStream_t>(stream);
 
     noallocSetupKernel<<<(unsigned)std::max<long long>(1, std::min<long long>(64, (nunits + 255) / 256)), 256, 0, s>>>(

@@ -34,6 +34,9 @@ enum SolverId { SOLVER_FWAVE = 1, SOLVER_AUGRIE = 2, SOLVER_HYBRID = 3, SOLVER_H
 enum Semantics { SEM_UNSPLIT = 0, SEM_SPLIT = 1 };
 enum BoundaryType { OUTFLOW = 0, WALL = 1, INFLOW = 2, CONNECT = 3, CONNECT_WITHIN_RANK = 4, PASSIVE = 5 };
 enum SplitDtMode { SPLIT_DT_MAX = 0, SPLIT_DT_LAST_EDGE = 1 };
+/// thread mapping of the sweep kernels: warp strips of 4, 2 or 1 rows per
+/// lane, or CTA tiles
+enum KernelVariant { VARIANT_WARP = 0, VARIANT_TILE = 1, VARIANT_WARP2 = 2, VARIANT_WARP1 = 3 };
 
 struct BlockDesc {
     int nx, ny;       // interior cells
@@ -58,8 +61,9 @@ struct WorkUnit {
 // time/steps/current buffer after the update pass.
 struct GroupState {
     unsigned int speedBits;  // max wave speed of the running step (float bits)
-    unsigned int arrived;    // CTAs of the running pass that have finished
-    int units;               // CTAs per pass in this group
+    unsigned int arrived;    // segments of the running pass that have finished
+    int units;               // segments of the speed pass in this group
+    int unitsUpd;            // segments of the update pass in this group
     int firstBlock;          // the group's first block (its dx, dy)
     float dt;                // maxTimestep of the last speed pass
     float speed;             // max wave speed of the last speed pass
@@ -81,6 +85,7 @@ struct DomainDev {
     GroupState *groups;
     int nblocks;
     int solver, semantics, splitDtMode;
+    int variant;             // KernelVariant
 };
 
 __device__ __forceinline__ float vmin(float a, float b) { return (b < a) ? b : a; }

@@ -17,11 +17,11 @@ cudaError_t launchSpeedAug(const DomainDev &d, int nunits, int threads, cudaStre
 cudaError_t launchUpdateAug(const DomainDev &d, int nunits, int threads, cudaStream_t s);
 
 // resident CTAs per SM of the step kernels (the smaller of the two passes)
-int occupancyFH(int solver, int sem, int threads);
-int occupancyAug(int solver, int sem, int threads);
-inline int stepOccupancy(int solver, int sem, int threads) {
-    return (solver == SOLVER_FWAVE || solver == SOLVER_HLLE) ? occupancyFH(solver, sem, threads)
-                                                           : occupancyAug(solver, sem, threads);
+int occupancyFH(int variant, int solver, int sem, bool update, int threads);
+int occupancyAug(int variant, int solver, int sem, bool update, int threads);
+inline int passOccupancy(int variant, int solver, int sem, bool update, int threads) {
+    return (solver == SOLVER_FWAVE || solver == SOLVER_HLLE) ? occupancyFH(variant, solver, sem, update, threads)
+                                                           : occupancyAug(variant, solver, sem, update, threads);
 }
 
 inline cudaError_t launchSpeed(const DomainDev &d, int nunits, int threads, cudaStream_t s) {

@@ -96,7 +96,7 @@ __device__ __forceinline__ void segmentDone(const DomainDev &d, GroupState *G, f
         if (!UPDATE) atomicMax(&G->speedBits, __float_as_uint(m));
         __threadfence();
         const unsigned prev = atomicAdd(&G->arrived, 1u);
-        *sLast = (prev == unsigned(G->units) - 1u);
+        *sLast = (prev == unsigned(UPDATE ? G->unitsUpd : G->units) - 1u);
     }
     __syncthreads();
     if (*sLast && threadIdx.x == 0) {

@@ -53,7 +53,8 @@ class Desc(C.Structure):
     _fields_ = [("blocks_x", C.c_int), ("blocks_y", C.c_int), ("nx_cols", C.POINTER(C.c_int)),
                 ("ny_rows", C.POINTER(C.c_int)), ("dx", C.c_float), ("dy", C.c_float),
                 ("boundary", C.c_int * 4), ("solver", C.c_int), ("semantics", C.c_int),
-                ("split_dt_mode", C.c_int), ("tile_rows", C.c_int), ("tile_cols", C.c_int), ("device", C.c_int)]
+                ("split_dt_mode", C.c_int), ("tile_rows", C.c_int), ("tile_cols", C.c_int), ("device", C.c_int),
+                ("kernel_variant", C.c_int)]
 
 
 _lib = None
@@ -190,7 +191,7 @@ class Domain:
     """Blocks of one simulation on the GPU (global time step)."""
 
     def __init__(self, nx_cols, ny_rows, dx, dy, boundary=(OUTFLOW,) * 4, solver=HLLE, semantics=UNSPLIT,
-                 split_dt_mode=SPLIT_DT_MAX, tile_rows=0, tile_cols=0, device=0):
+                 split_dt_mode=SPLIT_DT_MAX, tile_rows=0, tile_cols=0, device=0, kernel_variant=0):
         self.nx_cols = [int(v) for v in nx_cols]
         self.ny_rows = [int(v) for v in ny_rows]
         self.bx, self.by = len(self.nx_cols), len(self.ny_rows)
@@ -205,6 +206,7 @@ class Domain:
             d.boundary[i] = int(boundary[i])
         d.solver, d.semantics, d.split_dt_mode = int(solver), int(semantics), int(split_dt_mode)
         d.tile_rows, d.tile_cols, d.device = int(tile_rows), int(tile_cols), int(device)
+        d.kernel_variant = int(kernel_variant)
         self.handle = C.c_void_p()
         _check(lib().swe_gpu_domain_create(C.byref(d), C.byref(self.handle)))
         self.shapes = [(self.nx_cols[k // self.by], self.ny_rows[k % self.by]) for k in range(self.bx * self.by)]
