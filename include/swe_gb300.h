@@ -21,6 +21,8 @@
 #ifndef SWE_GB300_H
 #define SWE_GB300_H
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -110,6 +112,19 @@ int swe_gpu_download_block(swe_gpu_domain *dom, int block, float *h, float *hu, 
  * memory reaches full link bandwidth).  Both return when the copy is done. */
 int swe_gpu_upload_domain(swe_gpu_domain *dom, const float *h, const float *hu, const float *hv, const float *b);
 int swe_gpu_download_domain(swe_gpu_domain *dom, float *h, float *hu, float *hv, float *b);
+
+/* Checkpoint snapshot of one block without stopping the simulation: a device
+ * kernel writes the current interior of h, hu, hv as big-endian (y, x) slabs
+ * (the NetCDF record layout of NetCdfWriter::writeTimeStep,
+ * src/writer/NetCdfWriter.cpp:207-234) into a device staging area and
+ * copies them to the three host buffers (nx*ny*4 bytes each; pinned memory
+ * makes the copy asynchronous).  Returns at once; the data is there after
+ * swe_gpu_snapshot_wait.  Steps queued after the call do not disturb it. */
+int swe_gpu_snapshot_slabs_async(swe_gpu_domain *dom, int block, void *h, void *hu, void *hv);
+int swe_gpu_snapshot_wait(swe_gpu_domain *dom);
+/* page-locked host memory for snapshot and transfer buffers (cudaMallocHost) */
+int swe_gpu_alloc_pinned(size_t bytes, void **out);
+int swe_gpu_free_pinned(void *p);
 
 /* bathymetry ghosts: OUTFLOW/WALL copies (SWE_Block::applyBoundaryBathymetry,
  * src/blocks/SWE_Block.hh:724-749) and neighbour copies (exchangeBathymetry,

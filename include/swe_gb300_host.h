@@ -45,6 +45,20 @@ int swe_host_decompose(int nx, int ny, int nblocks, float dx, float dy, float or
                        int *blocks_x, int *blocks_y, int *nx_cols, int *ny_rows, float *origin_x_cols,
                        float *origin_y_rows);
 
+/* NetCDF snapshot files with the reference writer's variables and layout
+ * (src/writer/NetCdfWriter.cpp:84-234: time, x, y, ah(time,y,x), hu, hv,
+ * b(y,x)), written in the classic 64-bit-offset format without libnetcdf. */
+typedef struct swe_nc_writer swe_nc_writer;
+/* creates the file; b is the block's bathymetry in Float2D layout (stride ld) */
+int swe_nc_open(const char *path, int nx, int ny, float dx, float dy, float origin_x, float origin_y, const float *b,
+                int ld, swe_nc_writer **out);
+/* appends time t from host Float2D arrays (NetCdfWriter::writeTimeStep) */
+int swe_nc_write_step(swe_nc_writer *w, float t, const float *h, const float *hu, const float *hv, int ld);
+/* appends time t from big-endian (y, x) slabs of the interior, as produced on
+ * the device by swe_gpu_snapshot_slabs_async */
+int swe_nc_write_step_slabs(swe_nc_writer *w, float t, const void *h, const void *hu, const void *hv);
+int swe_nc_close(swe_nc_writer *w);
+
 #ifdef __cplusplus
 }
 #endif

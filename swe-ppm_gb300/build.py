@@ -15,9 +15,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libswe_gb300.so")
+DRIVER = os.path.join(OUT, "swe_gb300")
 
 CUDA_SOURCES = ["csrc/swe_capi.cu", "csrc/swe_kernels_fh.cu", "csrc/swe_kernels_aug.cu"]
-HOST_SOURCES = ["host/swe_host.cpp"]
+HOST_SOURCES = ["host/swe_host.cpp", "host/netcdf_writer.cpp"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-fmad=false", "-lineinfo", "-std=c++17",
               "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-I" + os.path.join(ROOT, "include")]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-I" + os.path.join(ROOT, "include"),
@@ -50,7 +51,7 @@ def _deps():
 def build(verbose=False, force=False):
     os.makedirs(OUT, exist_ok=True)
     deps = _deps()
-    if not force and not _stale(LIB, deps):
+    if not force and not _stale(LIB, deps) and not _stale(DRIVER, deps):
         return LIB
     nvcc = _nvcc()
     jobs = []
@@ -74,6 +75,9 @@ def build(verbose=False, force=False):
     with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
         list(ex.map(run, jobs))
     run([nvcc, "-shared", "-o", LIB] + objs + ["-lcudart"])
+    # the driver executable (reference drivers' flags), linked against the library
+    run(["g++"] + CXX_FLAGS + ["-o", DRIVER, os.path.join(HERE, "host", "swe_gb300_main.cpp"), "-L" + OUT,
+                               "-lswe_gb300", "-Wl,-rpath,$ORIGIN", "-pthread"])
     return LIB
 
 

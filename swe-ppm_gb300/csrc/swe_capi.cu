@@ -173,6 +173,34 @@ __global__ void repackKernel(const DomainDev d, float *stage, long long stageEle
     }
 }
 
+/// interior of the current state of block k as big-endian (y, x) slabs:
+/// out[f][j*nx + i] = field_f(i+1, j+1); 32 x 32 tiles transposed through
+/// shared memory so both the column reads and the row writes are coalesced
+__global__ void snapshotKernel(const DomainDev d, int k, uint32_t *out) {
+    __shared__ float tile[32][33];
+    const BlockDesc B = d.blocks[k];
+    const int cur = d.groups[B.group].cur;
+    const float *fields[3] = {cur ? d.h[1] : d.h[0], cur ? d.hu[1] : d.hu[0], cur ? d.hv[1] : d.hv[0]};
+    const int i0 = blockIdx.x * 32, j0 = blockIdx.y * 32;
+    const size_t slab = size_t(B.nx) * size_t(B.ny);
+    for (int f = 0; f < 3; f++) {
+        const float *F = fields[f] + B.base;
+        for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+            const int i = i0 + r, j = j0 + threadIdx.x;
+            if (i < B.nx && j < B.ny) tile[r][threadIdx.x] = F[size_t(i + 1) * size_t(B.pitch) + size_t(j + 1)];
+        }
+        __syncthreads();
+        for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+            const int j = j0 + r, i = i0 + threadIdx.x;
+            if (i < B.nx && j < B.ny) {
+                const uint32_t u = __float_as_uint(tile[threadIdx.x][r]);
+                out[size_t(f) * slab + size_t(j) * size_t(B.nx) + size_t(i)] = __byte_perm(u, 0, 0x0123);
+            }
+        }
+        __syncthreads();
+    }
+}
+
 } // namespace
 
 struct swe_gpu_domain {
@@ -207,6 +235,7 @@ struct swe_gpu_domain {
     int maxCols = 0;              // max nx+2 over blocks
     cudaGraphExec_t graph = nullptr;
     int graphSteps = 0;
+    cudaEvent_t snapEvent = nullptr;  // completion of the last snapshot copy
 };
 
 namespace {
@@ -265,6 +294,7 @@ int setTargets(swe_gpu_domain *D, float target) {
 
 void freeDomain(swe_gpu_domain *D) {
     if (D->graph) cudaGraphExecDestroy(D->graph);
+    if (D->snapEvent) cudaEventDestroy(D->snapEvent);
     for (int i = 0; i < 2; i++) {
         cudaFree(D->h[i]);
         cudaFree(D->hu[i]);
@@ -584,6 +614,46 @@ int swe_gpu_download_domain(swe_gpu_domain *dom, float *h, float *hu, float *hv,
     if (!dom) return fail(SWE_GPU_ERR_INVALID, "null domain handle");
     float *const host[4] = {h, hu, hv, b};
     return stageTransfer(dom, 0, int(dom->blocks.size()), host, dom->blocks[0].ny + 2, false, true);
+}
+
+int swe_gpu_snapshot_slabs_async(swe_gpu_domain *dom, int block, void *h, void *hu, void *hv) {
+    int rc = checkBlock(dom, block);
+    if (rc) return rc;
+    if (!h || !hu || !hv) return fail(SWE_GPU_ERR_INVALID, "null snapshot buffer");
+    CUDA_TRY(cudaSetDevice(dom->device));
+    const BlockDesc &B = dom->blocks[block];
+    // the staging area holds 4 fields of the whole domain; 3 interior slabs fit
+    uint32_t *out = reinterpret_cast<uint32_t *>(dom->stage);
+    const dim3 grid(unsigned((B.nx + 31) / 32), unsigned((B.ny + 31) / 32));
+    snapshotKernel<<<grid, dim3(32, 8), 0, dom->stream>>>(dom->dev, block, out);
+    CUDA_TRY(cudaGetLastError());
+    const size_t slab = size_t(B.nx) * size_t(B.ny) * 4;
+    CUDA_TRY(cudaMemcpyAsync(h, out, slab, cudaMemcpyDeviceToHost, dom->stream));
+    CUDA_TRY(cudaMemcpyAsync(hu, reinterpret_cast<char *>(out) + slab, slab, cudaMemcpyDeviceToHost, dom->stream));
+    CUDA_TRY(cudaMemcpyAsync(hv, reinterpret_cast<char *>(out) + 2 * slab, slab, cudaMemcpyDeviceToHost, dom->stream));
+    if (!dom->snapEvent) CUDA_TRY(cudaEventCreateWithFlags(&dom->snapEvent, cudaEventDisableTiming));
+    CUDA_TRY(cudaEventRecord(dom->snapEvent, dom->stream));
+    return SWE_GPU_OK;
+}
+
+int swe_gpu_snapshot_wait(swe_gpu_domain *dom) {
+    if (!dom) return fail(SWE_GPU_ERR_INVALID, "null domain handle");
+    if (!dom->snapEvent) return SWE_GPU_OK;
+    CUDA_TRY(cudaSetDevice(dom->device));
+    CUDA_TRY(cudaEventSynchronize(dom->snapEvent));
+    return SWE_GPU_OK;
+}
+
+int swe_gpu_alloc_pinned(size_t bytes, void **out) {
+    if (!out) return fail(SWE_GPU_ERR_INVALID, "null output pointer");
+    cudaError_t e = cudaMallocHost(out, bytes);
+    if (e != cudaSuccess) return fail(SWE_GPU_ERR_NOMEM, "cudaMallocHost(%zu): %s", bytes, cudaGetErrorString(e));
+    return SWE_GPU_OK;
+}
+
+int swe_gpu_free_pinned(void *p) {
+    CUDA_TRY(cudaFreeHost(p));
+    return SWE_GPU_OK;
 }
 
 int swe_gpu_exchange_bathymetry(swe_gpu_domain *dom) {

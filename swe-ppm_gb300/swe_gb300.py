@@ -41,6 +41,8 @@ EXPORTED = [
     "swe_gpu_compute_fluxes", "swe_gpu_update_unknowns", "swe_gpu_get_max_timestep", "swe_gpu_step",
     "swe_gpu_advance", "swe_gpu_get_time", "swe_gpu_set_time", "swe_gpu_sync", "swe_gpu_status",
     "swe_gpu_get_stream", "swe_gpu_set_stream", "swe_gpu_last_error", "swe_gpu_version", "swe_gpu_solve_edges", "swe_gpu_step_block_noalloc",
+    "swe_gpu_snapshot_slabs_async", "swe_gpu_snapshot_wait", "swe_gpu_alloc_pinned", "swe_gpu_free_pinned",
+    "swe_nc_open", "swe_nc_write_step", "swe_nc_write_step_slabs", "swe_nc_close",
     "swe_host_scenario_geometry", "swe_host_scenario_boundary", "swe_host_init_block", "swe_host_decompose",
 ]
 
@@ -99,6 +101,15 @@ def lib():
         L.swe_gpu_solve_edges.argtypes = [C.c_int, C.c_longlong] + [vp] * 11 + [vp]
         L.swe_gpu_step_block_noalloc.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, vp,
                                                  C.c_int] + [vp] * 7 + [vp, vp]
+        L.swe_gpu_snapshot_slabs_async.argtypes = [vp, C.c_int, vp, vp, vp]
+        L.swe_gpu_snapshot_wait.argtypes = [vp]
+        L.swe_gpu_alloc_pinned.argtypes = [C.c_size_t, C.POINTER(vp)]
+        L.swe_gpu_free_pinned.argtypes = [vp]
+        L.swe_nc_open.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, vp,
+                                  C.c_int, C.POINTER(vp)]
+        L.swe_nc_write_step.argtypes = [vp, C.c_float, vp, vp, vp, C.c_int]
+        L.swe_nc_write_step_slabs.argtypes = [vp, C.c_float, vp, vp, vp]
+        L.swe_nc_close.argtypes = [vp]
         L.swe_host_scenario_geometry.argtypes = [C.c_int, vp, C.c_int, C.c_int, vp]
         L.swe_host_scenario_boundary.argtypes = [C.c_int, vp, vp]
         L.swe_host_init_block.argtypes = [C.c_int, vp, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float,
@@ -305,6 +316,13 @@ class Domain:
         _check(lib().swe_gpu_get_stream(self.handle, C.byref(s)))
         return s.value
 
+    def snapshot_slabs(self, k, bufs):
+        """asynchronous big-endian (y, x) interior slabs of block k into 3 host buffers (addresses)"""
+        _check(lib().swe_gpu_snapshot_slabs_async(self.handle, int(k), *[C.c_void_p(b) for b in bufs]))
+
+    def snapshot_wait(self):
+        _check(lib().swe_gpu_snapshot_wait(self.handle))
+
     def set_stream(self, stream):
         """launch on an external cudaStream_t (int handle); None = own stream"""
         _check(lib().swe_gpu_set_stream(self.handle, C.c_void_p(stream or 0)))
@@ -326,3 +344,29 @@ def step_block_noalloc(solver, semantics, nx, ny, dx, dy, boundary, ld, ins, out
                                             *[C.c_void_p(p) for p in outs], C.byref(dt) if want_dt else None,
                                             C.c_void_p(stream or 0)))
     return dt.value if want_dt else None
+
+
+class NetCdfWriter:
+    """Block snapshot file with the reference writer's layout (ah/hu/hv(time,y,x), b(y,x))."""
+
+    def __init__(self, path, nx, ny, dx, dy, origin_x, origin_y, b):
+        self.nx, self.ny = nx, ny
+        bb = np.ascontiguousarray(b, dtype=np.float32).ravel()
+        self.h = C.c_void_p()
+        rc = lib().swe_nc_open(path.encode(), nx, ny, dx, dy, origin_x, origin_y, _p(bb), ny + 2, C.byref(self.h))
+        if rc != 0:
+            raise SweGpuError("swe_nc_open(%s) failed: %d" % (path, rc))
+
+    def write(self, t, h, hu, hv):
+        arrs = [np.ascontiguousarray(a, dtype=np.float32).ravel() for a in (h, hu, hv)]
+        if lib().swe_nc_write_step(self.h, float(t), *[_p(a) for a in arrs], self.ny + 2) != 0:
+            raise SweGpuError("swe_nc_write_step failed")
+
+    def write_slabs(self, t, h, hu, hv):
+        if lib().swe_nc_write_step_slabs(self.h, float(t), *[C.c_void_p(p) for p in (h, hu, hv)]) != 0:
+            raise SweGpuError("swe_nc_write_step_slabs failed")
+
+    def close(self):
+        if self.h:
+            lib().swe_nc_close(self.h)
+            self.h = None
