@@ -146,7 +146,7 @@ def cpu_baseline(seconds=12.0):
     _, threads = R.step_parallel(1)  # also calibrates
     t1 = time.perf_counter()
     per = max(t1 - t0, 1e-3)
-    n = max(1, min(200, int(seconds / per)))
+    n = max(1, min(10000, int(seconds / per)))
     t0 = time.perf_counter()
     R.step_parallel(n)
     el = time.perf_counter() - t0
