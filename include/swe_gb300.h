@@ -90,6 +90,10 @@ typedef struct swe_gpu_desc {
     int kernel_variant;  /* thread mapping of the sweep kernels: 0 = CTA tiles of
                             tile_rows rows (default), 1 / 2 / 3 = warp strips of
                             4 / 2 / 1 rows per lane */
+    int speed_pass;      /* 0 = bounded speed pass where available (f-wave or HLLE,
+                            unsplit step, CTA tiles): exact wave speeds only where
+                            the previous update's speed bounds can reach the
+                            maximum; 1 = every edge.  Both give the same dt. */
 } swe_gpu_desc;
 
 int swe_gpu_domain_create(const swe_gpu_desc *desc, swe_gpu_domain **out);
@@ -153,6 +157,9 @@ int swe_gpu_step(swe_gpu_domain *dom, int nsteps);
  * graph; returns the executed steps and the float time reached */
 int swe_gpu_advance(swe_gpu_domain *dom, float t_end, int max_steps, int *steps_done, float *t_now);
 int swe_gpu_get_time(swe_gpu_domain *dom, float *t, int *steps);
+/* Kernels this domain has enqueued so far (a replay of the captured step
+ * graph counts each of its kernel nodes); no synchronisation. */
+int swe_gpu_launch_count(const swe_gpu_domain *dom, long long *count);
 int swe_gpu_set_time(swe_gpu_domain *dom, float t);
 
 int swe_gpu_sync(swe_gpu_domain *dom);

@@ -152,7 +152,13 @@ __global__ void repackKernel(const DomainDev d, float *stage, long long stageEle
     // next step's boundary values; the block's state as the reference shows
     // it (ghosts set at the start of the last step) has them in the other buffer.
     const bool ahead = !toDevice && G->ghostsAhead;
-    if (toDevice && x == 0 && threadIdx.x == 0) G->ghostsAhead = 0;
+    if (toDevice && x == 0 && threadIdx.x == 0) {
+        G->ghostsAhead = 0;
+        if (fieldMask & 7) {
+            G->boundsValid[0] = 0;
+            G->boundsValid[1] = 0;
+        }
+    }
     float *fields[4] = {cur ? d.h[1] : d.h[0], cur ? d.hu[1] : d.hu[0], cur ? d.hv[1] : d.hv[0], d.b};
     float *other[4] = {cur ? d.h[0] : d.h[1], cur ? d.hu[0] : d.hu[1], cur ? d.hv[0] : d.hv[1], d.b};
     const int rows = B.ny + 2;
@@ -236,6 +242,14 @@ struct swe_gpu_domain {
     cudaGraphExec_t graph = nullptr;
     int graphSteps = 0;
     cudaEvent_t snapEvent = nullptr;  // completion of the last snapshot copy
+    bool bounded = false;             // bounded speed pass (f-wave / HLLE, unsplit, CTA tiles)
+    std::vector<TileInfo> tiles;      // bound tiles of all blocks
+    TileInfo *dTiles = nullptr;
+    unsigned int *dTileW = nullptr;   // 2 parities x tiles
+    unsigned long long *dTileKey = nullptr;
+    int gridB = 0;                    // CTAs of the bounded speed pass
+    long long launches = 0;           // kernels enqueued (graph replays: per kernel node)
+    long long graphKernels = 0;       // kernel nodes of the captured step graph
 };
 
 namespace {
@@ -245,14 +259,21 @@ int enqueueGhost(swe_gpu_domain *D, int bathymetry) {
     dim3 grid((D->maxPerimeter + threads - 1) / threads, unsigned(D->blocks.size()));
     ghostKernel<<<grid, threads, 0, D->stream>>>(D->dev, bathymetry);
     CUDA_TRY(cudaGetLastError());
+    D->launches++;
     return SWE_GPU_OK;
 }
 
 int enqueueSpeed(swe_gpu_domain *D) {
     DomainDev d = D->dev;
+    if (D->bounded) {
+        CUDA_TRY(launchSpeedBound(d, D->gridB, D->stream));
+        D->launches++;
+        return SWE_GPU_OK;
+    }
     d.units = D->dUnits;
     d.ctaSeg = D->dCtaSeg;
     CUDA_TRY(launchSpeed(d, D->grid, D->tileRows, D->stream));
+    D->launches++;
     return SWE_GPU_OK;
 }
 
@@ -261,6 +282,7 @@ int enqueueUpdate(swe_gpu_domain *D) {
     d.units = D->dUnitsU;
     d.ctaSeg = D->dCtaSegU;
     CUDA_TRY(launchUpdate(d, D->gridU, D->tileRows, D->stream));
+    D->launches++;
     D->ghostsValid = true;  // the update pass pushed the next ghost ring
     return SWE_GPU_OK;
 }
@@ -308,6 +330,9 @@ void freeDomain(swe_gpu_domain *D) {
     cudaFree(D->dUnitsU);
     cudaFree(D->dCtaSegU);
     cudaFree(D->dGroups);
+    cudaFree(D->dTiles);
+    cudaFree(D->dTileW);
+    cudaFree(D->dTileKey);
     if (D->ownStream) cudaStreamDestroy(D->ownStream);
     delete D;
 }
@@ -453,9 +478,58 @@ int swe_gpu_domain_create(const swe_gpu_desc *desc, swe_gpu_domain **out) {
             ctaSeg.push_back(int(units.size()));
         }
     }
+    // Bounded speed pass: bound tiles of 32 x 32 cells per block, numbered
+    // block by block, column of tiles by column of tiles
+    bool smallBlocks = true;
+    for (const BlockDesc &B : D->blocks) smallBlocks = smallBlocks && B.nx < 65535 && B.ny < 65535;
+    D->bounded = D->variant == VARIANT_TILE && D->semantics == SEM_UNSPLIT &&
+                 (D->solver == SOLVER_FWAVE || D->solver == SOLVER_HLLE) && desc->speed_pass == 0 && smallBlocks;
+    if (D->bounded) {
+        int base = 0;
+        for (BlockDesc &B : D->blocks) {
+            B.tileBase = base;
+            B.tilesY = (B.ny + kBoundTile - 1) / kBoundTile;
+            base += B.tilesY * ((B.nx + kBoundTile - 1) / kBoundTile);
+        }
+        auto tileId = [&](int k, int i, int j) { return D->blocks[k].tileBase + i * D->blocks[k].tilesY + j; };
+        auto tilesX = [&](int k) { return (D->blocks[k].nx + kBoundTile - 1) / kBoundTile; };
+        auto ghostSide = [&](const BlockDesc &B, int side, int nbTile) {
+            const int type = B.bnd[side];
+            if (type == CONNECT_WITHIN_RANK) return nbTile;
+            return (type == OUTFLOW || type == WALL) ? kNbrSelf : kNbrUnbounded;
+        };
+        for (int k = 0; k < int(D->blocks.size()); k++) {
+            const BlockDesc &B = D->blocks[k];
+            for (int i = 0; i < tilesX(k); i++)
+                for (int j = 0; j < B.tilesY; j++) {
+                    TileInfo T{};
+                    T.base = B.base;
+                    T.pitch = B.pitch;
+                    T.group = B.group;
+                    T.x0 = 1 + i * kBoundTile;
+                    T.x1 = std::min(T.x0 + kBoundTile, B.nx + 1);
+                    T.y0 = 1 + j * kBoundTile;
+                    T.y1 = std::min(T.y0 + kBoundTile, B.ny + 1);
+                    T.nx = B.nx;
+                    T.ny = B.ny;
+                    const int nL = B.nbr[0], nR = B.nbr[1], nB = B.nbr[2], nT = B.nbr[3];
+                    T.nbr[0] = i > 0 ? tileId(k, i - 1, j) : ghostSide(B, 0, nL >= 0 ? tileId(nL, tilesX(nL) - 1, j) : 0);
+                    T.nbr[1] = j > 0 ? tileId(k, i, j - 1)
+                                     : ghostSide(B, 2, nB >= 0 ? tileId(nB, i, D->blocks[nB].tilesY - 1) : 0);
+                    T.nbr[2] = T.x1 <= B.nx ? kNbrSelf : ghostSide(B, 1, nR >= 0 ? tileId(nR, 0, j) : 0);
+                    T.nbr[3] = T.y1 <= B.ny ? kNbrSelf : ghostSide(B, 3, nT >= 0 ? tileId(nT, i, 0) : 0);
+                    D->tiles.push_back(T);
+                }
+        }
+        int sms = 148;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, D->device);
+        const long long want = ((long long)D->tiles.size() + 7) / 8;
+        D->gridB = int(std::max(1LL, std::min(want, (long long)sms * std::max(1, occupancyBound(D->solver)))));
+    }
     GroupState g0{};
     g0.units = int(D->units.size());
     g0.unitsUpd = int(D->unitsU.size());
+    g0.tiles = int(D->tiles.size());
     g0.firstBlock = 0;
     g0.target = INFINITY;
     g0.dt = 0.f;
@@ -475,6 +549,11 @@ int swe_gpu_domain_create(const swe_gpu_desc *desc, swe_gpu_domain **out) {
     ok = ok && cudaMalloc(&D->dUnitsU, sizeof(WorkUnit) * D->unitsU.size()) == cudaSuccess;
     ok = ok && cudaMalloc(&D->dCtaSegU, sizeof(int) * D->ctaSegU.size()) == cudaSuccess;
     ok = ok && cudaMalloc(&D->dGroups, sizeof(GroupState) * D->ngroups) == cudaSuccess;
+    if (D->bounded) {
+        ok = ok && cudaMalloc(&D->dTiles, sizeof(TileInfo) * D->tiles.size()) == cudaSuccess;
+        ok = ok && cudaMalloc(&D->dTileW, sizeof(unsigned int) * 2 * D->tiles.size()) == cudaSuccess;
+        ok = ok && cudaMalloc(&D->dTileKey, sizeof(unsigned long long) * 2 * D->tiles.size()) == cudaSuccess;
+    }
     if (!ok) {
         cudaGetLastError();
         freeDomain(D);
@@ -492,6 +571,12 @@ int swe_gpu_domain_create(const swe_gpu_desc *desc, swe_gpu_domain **out) {
     cudaMemcpyAsync(D->dUnitsU, D->unitsU.data(), sizeof(WorkUnit) * D->unitsU.size(), cudaMemcpyHostToDevice, D->stream);
     cudaMemcpyAsync(D->dCtaSegU, D->ctaSegU.data(), sizeof(int) * D->ctaSegU.size(), cudaMemcpyHostToDevice, D->stream);
     cudaMemcpyAsync(D->dGroups, D->groupsInit.data(), sizeof(GroupState) * D->ngroups, cudaMemcpyHostToDevice, D->stream);
+    if (D->bounded) {
+        cudaMemcpyAsync(D->dTiles, D->tiles.data(), sizeof(TileInfo) * D->tiles.size(), cudaMemcpyHostToDevice,
+                        D->stream);
+        cudaMemsetAsync(D->dTileW, 0, sizeof(unsigned int) * 2 * D->tiles.size(), D->stream);
+        cudaMemsetAsync(D->dTileKey, 0, sizeof(unsigned long long) * 2 * D->tiles.size(), D->stream);
+    }
     e = cudaStreamSynchronize(D->stream);
     if (e != cudaSuccess) {
         freeDomain(D);
@@ -512,6 +597,11 @@ int swe_gpu_domain_create(const swe_gpu_desc *desc, swe_gpu_domain **out) {
     D->dev.semantics = D->semantics;
     D->dev.splitDtMode = D->splitDtMode;
     D->dev.variant = D->variant;
+    D->dev.tileRows = D->tileRows;
+    D->dev.tileW = D->dTileW;
+    D->dev.tileKey = D->dTileKey;
+    D->dev.tileInfo = D->dTiles;
+    D->dev.ntiles = int(D->tiles.size());
     *out = D;
     return SWE_GPU_OK;
 }
@@ -558,6 +648,7 @@ static int stageTransfer(swe_gpu_domain *D, int firstBlock, int nblocks, float *
     if (!up) {
         repackKernel<<<grid, 256, 0, D->stream>>>(D->dev, D->stage, D->stageElems, 0, mask, firstBlock);
         CUDA_TRY(cudaGetLastError());
+        D->launches++;
     }
     for (int f = 0; f < 4; f++) {
         if (!host[f]) continue;
@@ -578,6 +669,7 @@ static int stageTransfer(swe_gpu_domain *D, int firstBlock, int nblocks, float *
     if (up) {
         repackKernel<<<grid, 256, 0, D->stream>>>(D->dev, D->stage, D->stageElems, 1, mask, firstBlock);
         CUDA_TRY(cudaGetLastError());
+        D->launches++;
         D->ghostsValid = false;
     }
     if (wait) CUDA_TRY(cudaStreamSynchronize(D->stream));
@@ -627,6 +719,7 @@ int swe_gpu_snapshot_slabs_async(swe_gpu_domain *dom, int block, void *h, void *
     const dim3 grid(unsigned((B.nx + 31) / 32), unsigned((B.ny + 31) / 32));
     snapshotKernel<<<grid, dim3(32, 8), 0, dom->stream>>>(dom->dev, block, out);
     CUDA_TRY(cudaGetLastError());
+    dom->launches++;
     const size_t slab = size_t(B.nx) * size_t(B.ny) * 4;
     CUDA_TRY(cudaMemcpyAsync(h, out, slab, cudaMemcpyDeviceToHost, dom->stream));
     CUDA_TRY(cudaMemcpyAsync(hu, reinterpret_cast<char *>(out) + slab, slab, cudaMemcpyDeviceToHost, dom->stream));
@@ -711,8 +804,11 @@ int swe_gpu_advance(swe_gpu_domain *dom, float t_end, int max_steps, int *steps_
         cudaGraph_t g;
         CUDA_TRY(cudaStreamBeginCapture(dom->stream, cudaStreamCaptureModeThreadLocal));
         int rc = SWE_GPU_OK;
+        const long long before = dom->launches;
         for (int i = 0; i < batch && rc == SWE_GPU_OK; i++) rc = enqueueStep(dom);
         cudaError_t e = cudaStreamEndCapture(dom->stream, &g);
+        dom->graphKernels = dom->launches - before;  // captured, not launched
+        dom->launches = before;
         if (rc) return rc;
         if (e != cudaSuccess) return fail(SWE_GPU_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
         e = cudaGraphInstantiate(&dom->graph, g, 0);
@@ -731,6 +827,7 @@ int swe_gpu_advance(swe_gpu_domain *dom, float t_end, int max_steps, int *steps_
         const int remaining = max_steps - done;
         if (remaining >= dom->graphSteps) {
             CUDA_TRY(cudaGraphLaunch(dom->graph, dom->stream));
+            dom->launches += dom->graphKernels;
         } else {
             for (int i = 0; i < remaining; i++) {
                 rc = enqueueStep(dom);
@@ -747,6 +844,12 @@ int swe_gpu_advance(swe_gpu_domain *dom, float t_end, int max_steps, int *steps_
     if (steps_done) *steps_done = done;
     if (t_now) *t_now = g[0].time;
     if (g[0].status) return fail(SWE_GPU_ERR_DEVICE, "device status 0x%x (NaN wave speed)", g[0].status);
+    return SWE_GPU_OK;
+}
+
+int swe_gpu_launch_count(const swe_gpu_domain *dom, long long *count) {
+    if (!dom || !count) return fail(SWE_GPU_ERR_INVALID, "null argument");
+    *count = dom->launches;
     return SWE_GPU_OK;
 }
 
@@ -895,6 +998,7 @@ __global__ void noallocSetupKernel(NoAllocScratch *s, BlockDesc b, int tileRows,
         g.cur = 0;
         g.status = 0;
         g.ghostsAhead = 0;
+        g.boundsValid[0] = g.boundsValid[1] = 0;
         s->group = g;
         s->block = b;
     }

@@ -47,6 +47,8 @@ struct BlockDesc {
     int nbr[4];       // neighbour block ids (CONNECT_WITHIN_RANK) or -1
     float dx, dy;
     long long stage;  // offset of the block in the contiguous host-order layout
+    int tileBase;     // first bound tile of the block (bounded speed pass)
+    int tilesY;       // bound tiles per column of tiles: ceil(ny / 32)
 };
 
 // work unit of the sweep kernels: one block, rows [y0, y0+TY) x columns [x0, x1)
@@ -74,7 +76,30 @@ struct GroupState {
     int status;              // bit 0: NaN wave speed, bit 1: non-finite water height produced
     int ghostsAhead;         // 1: the current buffer's ghost ring already holds the next
                              // step's boundary values (pushed by the update pass)
+    // Bounded speed pass: boundsValid[p] = 1 when the bound tiles' speed
+    // bounds and sample keys of parity p describe the state in buffer p
+    int boundsValid[2];
+    int tiles;               // bound tiles of the group's blocks
 };
+
+// Bound tile of the bounded speed pass: 32 x 32 interior cells of a block,
+// cells [x0, x1) x [y0, y1) (block coordinates, ends exclusive).  It owns the
+// x-edges (x-1|x), x0 <= x < x1, and y-edges (y-1|y), y0 <= y < y1, plus the
+// block's right (nx|nx+1) and top (ny|ny+1) edges where x1 = nx+1 or
+// y1 = ny+1.  nbr[side] (LEFT, BOTTOM, RIGHT, TOP) names whose speed bound
+// covers the cells across the tile's side that these edges touch: a tile id,
+// kNbrSelf (the tile's own cells: a copy or mirror ghost, or no edge on that
+// side) or kNbrUnbounded (ghosts set elsewhere).
+struct TileInfo {
+    long long base;
+    int pitch, group;
+    int x0, x1, y0, y1;
+    int nx, ny;
+    int nbr[4];
+};
+constexpr int kNbrSelf = -1;
+constexpr int kNbrUnbounded = -2;
+constexpr int kBoundTile = 32;
 
 struct DomainDev {
     float *h[2], *hu[2], *hv[2];
@@ -86,6 +111,16 @@ struct DomainDev {
     int nblocks;
     int solver, semantics, splitDtMode;
     int variant;             // KernelVariant
+    int tileRows;            // TY of the CTA-tile mapping
+    // bounded speed pass (null when the full speed pass is used), two
+    // parities of ntiles entries each, parity p describing the state written
+    // into buffer p: tileW = float bits of the largest cell speed bound of the
+    // tile, tileKey = (those bits << 32) | x << 16 | y of a cell attaining it
+    // (block coordinates), 0 if none
+    unsigned int *tileW;
+    unsigned long long *tileKey;
+    const TileInfo *tileInfo;
+    int ntiles;
 };
 
 __device__ __forceinline__ float vmin(float a, float b) { return (b < a) ? b : a; }

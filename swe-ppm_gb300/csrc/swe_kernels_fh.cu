@@ -1,5 +1,6 @@
 // Step kernels instantiated for the f-wave and HLLE solvers.
 #include "swe_launch.hpp"
+#include "swe_bound.cuh"
 #include "swe_warp.cuh"
 
 namespace swegb {
@@ -58,6 +59,14 @@ cudaError_t launchUpdateFH(const DomainDev &d, int n, int th, cudaStream_t s) {
     return d.solver == SOLVER_FWAVE ? update<SOLVER_FWAVE>(d, n, th, s) : update<SOLVER_HLLE>(d, n, th, s);
 }
 
+cudaError_t launchSpeedBound(const DomainDev &d, int grid, cudaStream_t s) {
+    if (d.solver == SOLVER_FWAVE)
+        speedBoundKernel<SOLVER_FWAVE><<<grid, 256, 0, s>>>(d);
+    else
+        speedBoundKernel<SOLVER_HLLE><<<grid, 256, 0, s>>>(d);
+    return cudaGetLastError();
+}
+
 template <class K> static int occ(K kernel, int th) {
     int a = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, kernel, th, 0);
@@ -83,6 +92,10 @@ template <int S> static int occupancy(int variant, int sem, bool upd, int th) {
 int occupancyFH(int variant, int solver, int sem, bool update, int threads) {
     return solver == SOLVER_FWAVE ? occupancy<SOLVER_FWAVE>(variant, sem, update, threads)
                            : occupancy<SOLVER_HLLE>(variant, sem, update, threads);
+}
+
+int occupancyBound(int solver) {
+    return solver == SOLVER_FWAVE ? occ(speedBoundKernel<SOLVER_FWAVE>, 256) : occ(speedBoundKernel<SOLVER_HLLE>, 256);
 }
 
 } // namespace swegb

@@ -16,6 +16,11 @@ cudaError_t launchUpdateFH(const DomainDev &d, int nunits, int threads, cudaStre
 cudaError_t launchSpeedAug(const DomainDev &d, int nunits, int threads, cudaStream_t s);
 cudaError_t launchUpdateAug(const DomainDev &d, int nunits, int threads, cudaStream_t s);
 
+// bounded speed pass of the f-wave and HLLE unsplit step over the bound
+// tiles (d.tileInfo, d.tileW, d.tileKey), 256 threads per CTA
+cudaError_t launchSpeedBound(const DomainDev &d, int grid, cudaStream_t s);
+int occupancyBound(int solver);
+
 // resident CTAs per SM of the step kernels (the smaller of the two passes)
 int occupancyFH(int variant, int solver, int sem, bool update, int threads);
 int occupancyAug(int variant, int solver, int sem, bool update, int threads);

@@ -107,6 +107,9 @@ __device__ __forceinline__ void segmentDone(const DomainDev &d, GroupState *G, f
             G->steps = G->steps + 1;
             G->cur = cur ^ 1;
             G->ghostsAhead = 1;
+            // speed bounds now describe the output buffer
+            G->boundsValid[cur] = 0;
+            G->boundsValid[cur ^ 1] = d.tileW ? 1 : 0;
         } else {
             float s = __uint_as_float(atomicOr(&G->speedBits, 0u));
             const BlockDesc &F = d.blocks[G->firstBlock];
@@ -149,6 +152,50 @@ __device__ __forceinline__ void segmentDone(const DomainDev &d, GroupState *G, f
         __threadfence();
     }
 }
+
+/// Upper bound of the wave speed of any f-wave / HLLE edge touching a cell:
+/// max(|hu|, |hv|)/h + sqrt(g h) for wet cells, 0 for dry ones (a dry side
+/// takes the mirrored wet state).  The Roe speed |uRoe| + cRoe of an edge is at
+/// most the sqrt(h)-weighted mean of its two cells' |u| + c (cRoe <= that mean
+/// of c by the quadratic-arithmetic mean inequality), and the Einfeldt speeds
+/// u_L - c_L, u_R + c_R are bounded by the cells' own values, so every edge
+/// speed is at most the larger bound of its two cells.  Approximate reciprocal
+/// and square root: the bound is used with a relative margin far above their
+/// error; non-finite or huge states give +inf (never skipped).
+__device__ __forceinline__ float cellSpeedBound(float h, float hu, float hv) {
+    if (h < kDryTol) return 0.f;
+    const float m = fmaxf(fabsf(hu), fabsf(hv));
+    const float w = fmaf(m, __fdividef(1.f, h), kSqrtG * (h * rsqrtf(h)));
+    return (w <= FLT_MAX && h < 1e30f) ? w : INFINITY;
+}
+
+/// folds the warp's cell bounds since the last flush into bound tile
+/// (column of cell xcell, rows of the warp) of parity `out` (all lanes call)
+__device__ __forceinline__ void boundFlush(const DomainDev &d, const BlockDesc &B, int out, int xcell, int warpRow0,
+                                           int yTop, int y, float &wmax, int &xarg) {
+    unsigned long long key = (wmax > 0.f && xarg >= 0)
+                                 ? ((unsigned long long)__float_as_uint(wmax) << 32) |
+                                       ((unsigned long long)xarg << 16) | (unsigned long long)y
+                                 : 0ull;
+    float wm = wmax;
+    for (int o = 16; o > 0; o >>= 1) {
+        wm = vmax(wm, __shfl_xor_sync(0xffffffffu, wm, o));
+        const unsigned long long k2 = __shfl_xor_sync(0xffffffffu, key, o);
+        key = k2 > key ? k2 : key;
+    }
+    if ((threadIdx.x & 31) == 0 && warpRow0 <= yTop && wm > 0.f) {
+        const size_t tile = size_t(out) * size_t(d.ntiles) + size_t(B.tileBase) +
+                            size_t((xcell - 1) / kBoundTile) * size_t(B.tilesY) + size_t((warpRow0 - 1) / kBoundTile);
+        atomicMax(&d.tileW[tile], __float_as_uint(wm));
+        atomicMax(&d.tileKey[tile], key);
+    }
+    wmax = 0.f;
+    xarg = -1;
+}
+
+/// relative margin of the speed bounds (rounding of the bound and of the
+/// edge speeds is a few ulp)
+constexpr float kBoundMargin = 1.0f + 1.0f / 4096.0f;
 
 /// pushes Q^{n+1} of a cell on the block's rim into every ghost cell whose
 /// value the next step's setGhostLayer takes from it (kept out of line: only
@@ -207,13 +254,17 @@ __device__ __forceinline__ void storeCell(const DomainDev &d, const BlockDesc &B
 }
 
 template <int S, int SEM, bool UPDATE>
-__global__ void __launch_bounds__(kMaxTileRows) sweepKernel(const DomainDev d) {
+__global__ void __launch_bounds__(kMaxTileRows, 4) sweepKernel(const DomainDev d) {
+    // the update pass of the f-wave / HLLE unsplit step also records the
+    // speed bounds of the bounded speed pass
+    constexpr bool BOUNDS = UPDATE && SEM == SEM_UNSPLIT && (S == SOLVER_HLLE || S == SOLVER_FWAVE);
     __shared__ float sC[2][6][kMaxTileRows];   // y-direction cell quantities of column x
     __shared__ float sR[2][2][kMaxTileRows];   // right-going (h, hv) update into row t
     __shared__ float sBot[2][kMaxTileCols];    // right-going update into row y0 (bottom tile edge)
     __shared__ float sTop[2][kMaxTileCols];    // left-going update into row yTop (top tile edge)
     __shared__ float sRed[kMaxTileRows / 32];
     __shared__ int sLast;
+    const bool bounds = BOUNDS && d.tileW != nullptr;
 
     const int t = threadIdx.x, TY = blockDim.x;
     const int segEnd = d.ctaSeg[blockIdx.x + 1];
@@ -276,6 +327,8 @@ __global__ void __launch_bounds__(kMaxTileRows) sweepKernel(const DomainDev d) {
         float oldH = 0.f, oldHU = 0.f, oldHV = 0.f;  // Q^n of cell x-1
         float syH = 0.f, syHV = 0.f;                 // y net-update sums of cell x-1
         bool bad = false;                            // a non-finite water height was produced
+        float wmax = 0.f;                            // largest speed bound of this row's new cells
+        int xarg = -1;                               // ... and its column
 
         for (int x = x0 - 1; x <= x1; ++x) {
             const float ch = nh, chu = nhu, chv = nhv, cb = nb;
@@ -311,6 +364,13 @@ __global__ void __launch_bounds__(kMaxTileRows) sweepKernel(const DomainDev d) {
                             hvn = oldHV - dtdx * syHV;
                         }
                         bad |= !(fabsf(hn) <= FLT_MAX);
+                        if (BOUNDS) {
+                            const float w = cellSpeedBound(hn, hun, hvn);
+                            if (w > wmax) {
+                                wmax = w;
+                                xarg = x - 1;
+                            }
+                        }
                         storeCell(d, B, cur ^ 1, P, x - 1, y, hn, hun, hvn);
                     }
                     pendH = aR;
@@ -319,6 +379,9 @@ __global__ void __launch_bounds__(kMaxTileRows) sweepKernel(const DomainDev d) {
                     smax = vmax(smax, edgeSpeed<S>(prevX, cx));
                 }
             }
+            // cell x-1 closed a column range of bound tiles, or the segment
+            if (BOUNDS && bounds && x - 1 >= x0 && (((x - 2) & (kBoundTile - 1)) == kBoundTile - 1 || x == x1))
+                boundFlush(d, B, cur ^ 1, x - 1, y0 + (t & ~31), yTop, y, wmax, xarg);
             prevX = cx;
 
             // y-edges of column x

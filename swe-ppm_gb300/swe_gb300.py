@@ -42,6 +42,7 @@ EXPORTED = [
     "swe_gpu_advance", "swe_gpu_get_time", "swe_gpu_set_time", "swe_gpu_sync", "swe_gpu_status",
     "swe_gpu_get_stream", "swe_gpu_set_stream", "swe_gpu_last_error", "swe_gpu_version", "swe_gpu_solve_edges", "swe_gpu_step_block_noalloc",
     "swe_gpu_snapshot_slabs_async", "swe_gpu_snapshot_wait", "swe_gpu_alloc_pinned", "swe_gpu_free_pinned",
+    "swe_gpu_launch_count",
     "swe_nc_open", "swe_nc_write_step", "swe_nc_write_step_slabs", "swe_nc_close",
     "swe_host_scenario_geometry", "swe_host_scenario_boundary", "swe_host_init_block", "swe_host_decompose",
 ]
@@ -56,7 +57,7 @@ class Desc(C.Structure):
                 ("ny_rows", C.POINTER(C.c_int)), ("dx", C.c_float), ("dy", C.c_float),
                 ("boundary", C.c_int * 4), ("solver", C.c_int), ("semantics", C.c_int),
                 ("split_dt_mode", C.c_int), ("tile_rows", C.c_int), ("tile_cols", C.c_int), ("device", C.c_int),
-                ("kernel_variant", C.c_int)]
+                ("kernel_variant", C.c_int), ("speed_pass", C.c_int)]
 
 
 _lib = None
@@ -94,6 +95,7 @@ def lib():
         L.swe_gpu_step.argtypes = [vp, C.c_int]
         L.swe_gpu_advance.argtypes = [vp, C.c_float, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_float)]
         L.swe_gpu_get_time.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_int)]
+        L.swe_gpu_launch_count.argtypes = [vp, C.POINTER(C.c_longlong)]
         L.swe_gpu_set_time.argtypes = [vp, C.c_float]
         L.swe_gpu_status.argtypes = [vp, C.POINTER(C.c_int)]
         L.swe_gpu_get_stream.argtypes = [vp, C.POINTER(vp)]
@@ -202,7 +204,7 @@ class Domain:
     """Blocks of one simulation on the GPU (global time step)."""
 
     def __init__(self, nx_cols, ny_rows, dx, dy, boundary=(OUTFLOW,) * 4, solver=HLLE, semantics=UNSPLIT,
-                 split_dt_mode=SPLIT_DT_MAX, tile_rows=0, tile_cols=0, device=0, kernel_variant=0):
+                 split_dt_mode=SPLIT_DT_MAX, tile_rows=0, tile_cols=0, device=0, kernel_variant=0, speed_pass=0):
         self.nx_cols = [int(v) for v in nx_cols]
         self.ny_rows = [int(v) for v in ny_rows]
         self.bx, self.by = len(self.nx_cols), len(self.ny_rows)
@@ -218,6 +220,7 @@ class Domain:
         d.solver, d.semantics, d.split_dt_mode = int(solver), int(semantics), int(split_dt_mode)
         d.tile_rows, d.tile_cols, d.device = int(tile_rows), int(tile_cols), int(device)
         d.kernel_variant = int(kernel_variant)
+        d.speed_pass = int(speed_pass)
         self.handle = C.c_void_p()
         _check(lib().swe_gpu_domain_create(C.byref(d), C.byref(self.handle)))
         self.shapes = [(self.nx_cols[k // self.by], self.ny_rows[k % self.by]) for k in range(self.bx * self.by)]
@@ -299,6 +302,12 @@ class Domain:
         t, n = C.c_float(), C.c_int()
         _check(lib().swe_gpu_get_time(self.handle, C.byref(t), C.byref(n)))
         return t.value, n.value
+
+    def launch_count(self):
+        """kernels this domain has enqueued so far"""
+        n = C.c_longlong()
+        _check(lib().swe_gpu_launch_count(self.handle, C.byref(n)))
+        return n.value
 
     def set_time(self, t):
         _check(lib().swe_gpu_set_time(self.handle, float(t)))
