@@ -160,6 +160,10 @@ int swe_gpu_get_time(swe_gpu_domain *dom, float *t, int *steps);
 /* Kernels this domain has enqueued so far (a replay of the captured step
  * graph counts each of its kernel nodes); no synchronisation. */
 int swe_gpu_launch_count(const swe_gpu_domain *dom, long long *count);
+/* Bounded speed pass: bound tiles of the domain and how many of them the
+ * last pass evaluated edge by edge (both 0 when the full speed pass is in
+ * use).  Synchronises the domain's stream. */
+int swe_gpu_speed_pass_stats(swe_gpu_domain *dom, int *tiles, int *evaluated);
 int swe_gpu_set_time(swe_gpu_domain *dom, float t);
 
 int swe_gpu_sync(swe_gpu_domain *dom);

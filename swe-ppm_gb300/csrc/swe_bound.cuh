@@ -11,14 +11,17 @@
 //    its left / bottom (and, on the block's rim, right / top) side, so its
 //    speed is at most the largest of those tiles' bounds (the ghosts of wall
 //    and outflow sides copy the tile's own cells; other ghosts are unbounded);
-//  - each warp takes one tile: it evaluates exactly one edge at the tile's
-//    largest bound and adds that speed to the group's running maximum at once;
-//    the running maximum T read afterwards is the speed of some edge, hence a
-//    lower bound of the step's maximum;
+//  - each warp takes one tile and evaluates exactly the edge at the tile's
+//    largest bound, and the fastest edge of the last pass; the largest of
+//    these exact speeds within the CTA is a lower bound T of the maximum;
 //  - the tile's edges are evaluated only when its bound times a small margin
 //    reaches T.
 // Every skipped edge is slower than T, so the maximum over the evaluated
-// edges is the maximum over all edges, whatever order the warps run in.
+// edges is the maximum over all edges.  The last pass's fastest edge moves
+// little between steps, so T is almost always within a few ulp of the new
+// maximum and only the tiles that can reach it are evaluated.  Group state is
+// read through the read-only path and the pass's atomics touch one key and
+// one counter per CTA, so no cache line serialises the grid.
 // Without valid bounds (first step, after an upload) every edge is evaluated.
 //
 // The pass also clears the other parity's tile entries for the update pass
@@ -34,32 +37,61 @@ __device__ __forceinline__ void cellAt(const float *H, const float *HU, const fl
     cellQuantities<S>(H[o], HU[o], HV[o], 0.f, cx, cy);
 }
 
-/// exact speed of one edge next to interior cell (x, y) of a block: the
-/// x-edge to its left neighbour (right neighbour in column 1), else the
-/// y-edge below (above in row 1); -1 for a 1 x 1 block
+/// speed of the edge between the cells at element offsets oa (left / below)
+/// and ob (right / above) of the current buffer; dir 0: x-edge, 1: y-edge
 template <int S>
-__device__ __forceinline__ float sampleEdgeSpeed(const float *H, const float *HU, const float *HV, size_t P, int x,
-                                                 int y, int nx, int ny) {
-    int xa = x, ya = y, xb = x, yb = y;
-    bool alongX = true;
-    if (x > 1) xa = x - 1;
-    else if (nx > 1) xb = x + 1;
-    else if (y > 1) { ya = y - 1; alongX = false; }
-    else if (ny > 1) { yb = y + 1; alongX = false; }
-    else return -1.f;
+__device__ __forceinline__ float edgeSpeedAt(const float *H, const float *HU, const float *HV, long long oa,
+                                             long long ob, int dir) {
     Cell ax, ay, bx, by;
-    cellAt<S>(H, HU, HV, size_t(xa) * P + size_t(ya), ax, ay);
-    cellAt<S>(H, HU, HV, size_t(xb) * P + size_t(yb), bx, by);
-    return alongX ? edgeSpeed<S>(ax, bx) : edgeSpeed<S>(ay, by);
+    cellQuantities<S>(__ldg(H + oa), __ldg(HU + oa), __ldg(HV + oa), 0.f, ax, ay);
+    cellQuantities<S>(__ldg(H + ob), __ldg(HU + ob), __ldg(HV + ob), 0.f, bx, by);
+    return dir ? edgeSpeed<S>(ay, by) : edgeSpeed<S>(ax, bx);
 }
 
-/// exact maximum speed of the edges of columns [xa, xb) of a tile: x-edges
-/// (x-1|x) and the y-edges of those columns (the block's top edge in the top
-/// rim tile), plus (nx|nx+1) when xb = nx+1; lane = row y0 + lane, the loads
-/// of all (at most NB) columns issued together
+/// code of the edge whose right / upper cell is (x, y) of bound tile `tile`
+__device__ __forceinline__ unsigned int edgeCode(long long tile, const TileInfo &I, int x, int y, int dir) {
+    return (unsigned(tile) << 13) | (unsigned(dir) << 12) | (unsigned(x - I.x0) << 6) | unsigned(y - I.y0);
+}
+
+/// the sample edge next to interior cell (x, y) of a block: the x-edge to its
+/// left neighbour (right neighbour in column 1), else the y-edge below (above
+/// in row 1); false for a 1 x 1 block.  Offsets include the block's base.
+__device__ __forceinline__ bool sampleEdge(const TileInfo &I, long long tile, int x, int y, long long &oa,
+                                           long long &ob, int &dir, unsigned int &code) {
+    const long long P = I.pitch;
+    int xb = x, yb = y;
+    dir = 0;
+    if (x > 1) {
+    } else if (I.nx > 1) {
+        xb = x + 1;
+    } else if (y > 1) {
+        dir = 1;
+    } else if (I.ny > 1) {
+        yb = y + 1;
+        dir = 1;
+    } else {
+        return false;
+    }
+    ob = I.base + xb * P + yb;
+    oa = dir ? ob - 1 : ob - P;
+    code = edgeCode(tile, I, xb, yb, dir);
+    return true;
+}
+
+__device__ __forceinline__ unsigned long long speedKey(float s, unsigned int code) {
+    return ((unsigned long long)__float_as_uint(s) << 32) | code;
+}
+__device__ __forceinline__ unsigned long long umax64(unsigned long long a, unsigned long long b) { return a > b ? a : b; }
+
+/// exact speeds of the edges of columns [xa, xb) of a tile: x-edges (x-1|x)
+/// and the y-edges of those columns (the block's top edge in the top rim
+/// tile), plus (nx|nx+1) when xb = nx+1; lane = row y0 + lane, the loads of
+/// all (at most NB) columns issued together.  Returns the lane's fastest edge
+/// as a speed key.
 template <int S>
-__device__ __forceinline__ float tileColumnsSpeed(const float *H, const float *HU, const float *HV, size_t P,
-                                                  const TileInfo &I, int xa, int xb, int lane) {
+__device__ __forceinline__ unsigned long long tileColumnsSpeed(const float *H, const float *HU, const float *HV,
+                                                               size_t P, const TileInfo &I, long long tile, int xa,
+                                                               int xb, int lane) {
     constexpr int NB = 4;
     const int y = I.y0 + lane;
     const bool active = y < I.y1;
@@ -82,7 +114,7 @@ __device__ __forceinline__ float tileColumnsSpeed(const float *H, const float *H
             }
         }
     }
-    float smax = 0.f;
+    unsigned long long best = 0ull;
     Cell prevX, dummy;
     cellQuantities<S>(h[0], hu[0], hv[0], 0.f, prevX, dummy);
 #pragma unroll
@@ -98,140 +130,194 @@ __device__ __forceinline__ float tileColumnsSpeed(const float *H, const float *H
         below.c = __shfl_up_sync(0xffffffffu, cy.c, 1);
         below.b = 0.f;
         if (active) {
-            smax = vmax(smax, edgeSpeed<S>(prevX, cx));  // x-edge (x-1 | x)
-            if (k <= NB && x < xb) {                     // a column of the tile: its y-edges
+            const float sx = edgeSpeed<S>(prevX, cx);  // x-edge (x-1 | x)
+            if (sx > 0.f) best = umax64(best, speedKey(sx, edgeCode(tile, I, x, y, 0)));
+            if (k <= NB && x < xb) {                   // a column of the tile: its y-edges
                 if (lane == 0) cellQuantities<S>(hB[k - 1], 0.f, hvB[k - 1], 0.f, dummy, below);
-                smax = vmax(smax, edgeSpeed<S>(below, cy));
+                const float sy = edgeSpeed<S>(below, cy);
+                if (sy > 0.f) best = umax64(best, speedKey(sy, edgeCode(tile, I, x, y, 1)));
                 if (top) {
                     Cell above;
                     cellQuantities<S>(hT[k - 1], 0.f, hvT[k - 1], 0.f, dummy, above);
-                    smax = vmax(smax, edgeSpeed<S>(cy, above));
+                    const float st = edgeSpeed<S>(cy, above);
+                    if (st > 0.f) best = umax64(best, speedKey(st, edgeCode(tile, I, x, y + 1, 1)));
                 }
             }
         }
         prevX = cx;
     }
-    return smax;
+    return best;
 }
 
-/// the group's speed pass is done when `count` more tiles are: max speed ->
-/// dt (src/blocks/SWE_DimensionalSplittingMpi.cpp:448-456)
-__device__ __forceinline__ void boundTilesDone(const DomainDev &d, GroupState *G, float m, int count) {
-    atomicMax(&G->speedBits, __float_as_uint(m));
+/// `count` more of the group's tiles are done, with their fastest edge `key`;
+/// the last one sets maxTimestep (src/blocks/SWE_DimensionalSplittingMpi.cpp:448-456)
+/// and remembers where the fastest edge was
+__device__ __forceinline__ void boundTilesDone(const DomainDev &d, GroupState *G, unsigned long long key, int count) {
+    if (key) atomicMax(&G->maxEdge, key);
     __threadfence();
     const unsigned prev = atomicAdd(&G->arrived, unsigned(count));
     if (prev + unsigned(count) == unsigned(G->tiles)) {
         __threadfence();
-        const float s = __uint_as_float(atomicOr(&G->speedBits, 0u));
+        const unsigned long long k = atomicOr(&G->maxEdge, 0ull);
+        const float s = __uint_as_float(unsigned(k >> 32));  // every evaluated edge is in the key's maximum
+        if (k) {
+            const unsigned code = unsigned(k);
+            const TileInfo I = d.tileInfo[code >> 13];
+            const int dir = (code >> 12) & 1;
+            const long long x = I.x0 + ((code >> 6) & 63), y = I.y0 + (code & 63);
+            G->prevB = I.base + x * I.pitch + y;
+            G->prevA = dir ? G->prevB - 1 : G->prevB - I.pitch;
+            G->prevDir = dir;
+            G->prevValid = 1;
+        }
         const BlockDesc &F = d.blocks[G->firstBlock];
         G->speed = s;
         G->dt = timestepFromSpeed(s, F.dx, F.dy, SEM_UNSPLIT);
         if (!(s == s)) G->status |= 1;
+        G->lastCandidates = atomicAdd(&G->candidates, 0);
+        G->candidates = 0;
         G->speedBits = 0u;
+        G->maxEdge = 0ull;
         G->arrived = 0u;
         __threadfence();
     }
 }
 
-// One round = one tile per warp.  Each warp reads its tile's bound, samples
-// one exact edge speed and decides; the CTA's candidate tiles are then
-// evaluated by all its warps together, 4 columns per warp, so that a
-// candidate costs a couple of memory latencies instead of a lone warp's
-// serial march over 32 columns.
+// One round = one tile per warp.  Lanes 0 and 1 of each warp evaluate, side
+// by side, the tile's sample edge and the last pass's fastest edge; every warp
+// compares its tile's bound with the CTA's largest sample in the same group.
+// The CTA's candidate tiles are then evaluated by all its warps together, 4
+// columns per warp.
 template <int S> __global__ void __launch_bounds__(256, 4) speedBoundKernel(const DomainDev d) {
-    __shared__ float sMax[8], sRed[8];
-    __shared__ int sGrp[8], sCnt[8];
+    __shared__ float sSamp[8], sW[8];
+    __shared__ int sGrp[8], sCnt[8], sTileGrp[8];
+    __shared__ unsigned long long sKey[8];
     __shared__ int sCand[8], sNCand;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int nwb = int(blockDim.x >> 5);
     int grp = -1, cnt = 0;
-    float smax = 0.f;
+    unsigned long long bkey = 0ull;  // lane 0: the warp's fastest edge so far (group grp)
     for (long long round = 0;; round++) {
         // consecutive tiles go to different CTAs
         const long long first = (long long)blockIdx.x + (long long)gridDim.x * (round * nwb);
         if (first >= d.ntiles) break;
         if (threadIdx.x == 0) sNCand = 0;
-        __syncthreads();
-        const long long it = first + (long long)gridDim.x * wib;
-        if (it < d.ntiles) {
+        const long long slot = first + (long long)gridDim.x * wib;
+        // 1. bound and exact samples.  Tiles are dealt out by a multiplicative
+        // hash so that neighbouring candidates land on different CTAs; the
+        // loads of the bound, the key and the group state are issued together
+        // (both parities, selected afterwards), so the chain is: tile record,
+        // bounds and group state, sample cells.
+        const long long it = slot < d.ntiles ? (long long)((unsigned long long)slot * d.tileHashMul % (unsigned long long)d.ntiles) : slot;
+        int tgrp = -1;
+        float W = INFINITY, samp = 0.f;
+        if (slot < d.ntiles) {
             const TileInfo I = d.tileInfo[it];
             if (I.group != grp) {
-                if (grp >= 0 && cnt > 0) {
-                    float m = smax;
-                    for (int o = 16; o > 0; o >>= 1) m = vmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-                    if (lane == 0) boundTilesDone(d, d.groups + grp, m, cnt);
-                }
+                if (grp >= 0 && cnt > 0 && lane == 0) boundTilesDone(d, d.groups + grp, bkey, cnt);
                 grp = I.group;
                 cnt = 0;
-                smax = 0.f;
+                bkey = 0ull;
             }
-            GroupState *G = d.groups + grp;
-            if (groupActive(G)) {
-                cnt++;
-                const int cur = G->cur;
-                const bool valid = G->boundsValid[cur] != 0;
-                const unsigned int *Wp = d.tileW + size_t(cur) * size_t(d.ntiles);
-                float W = INFINITY;
-                unsigned long long key = 0ull;
-                if (valid) {
-                    W = __uint_as_float(Wp[it]);
-                    for (int s = 0; s < 4; s++) {
-                        const int n = I.nbr[s];
-                        if (n >= 0) W = vmax(W, __uint_as_float(Wp[n]));
-                        else if (n == kNbrUnbounded) W = INFINITY;
+            const GroupState *G = d.groups + grp;
+            // group state (constant during the pass: read-only path, one L2
+            // fetch per SM) and both parities of the tile entries at once
+            const float gTime = __ldg(&G->time), gTarget = __ldg(&G->target);
+            const int cur = __ldg(&G->cur), bv0 = __ldg(&G->boundsValid[0]), bv1 = __ldg(&G->boundsValid[1]);
+            const int pValid = __ldg(&G->prevValid), pDir = __ldg(&G->prevDir);
+            const long long pA = __ldg(&G->prevA), pB = __ldg(&G->prevB);
+            float w0 = 0.f, w1 = 0.f;
+            unsigned long long k0 = 0ull, k1 = 0ull;
+            if (lane == 0) {
+                w0 = __uint_as_float(__ldg(&d.tileW[it]));
+                w1 = __uint_as_float(__ldg(&d.tileW[size_t(d.ntiles) + size_t(it)]));
+                for (int sd = 0; sd < 4; sd++) {
+                    const int n = I.nbr[sd];
+                    if (n >= 0) {
+                        w0 = vmax(w0, __uint_as_float(__ldg(&d.tileW[n])));
+                        w1 = vmax(w1, __uint_as_float(__ldg(&d.tileW[size_t(d.ntiles) + size_t(n)])));
+                    } else if (n == kNbrUnbounded) {
+                        w0 = INFINITY;
+                        w1 = INFINITY;
                     }
-                    key = d.tileKey[size_t(cur) * size_t(d.ntiles) + size_t(it)];
                 }
-                if (lane == 0) {  // clear the entry the next update pass folds into
+                k0 = __ldg(&d.tileKey[it]);
+                k1 = __ldg(&d.tileKey[size_t(d.ntiles) + size_t(it)]);
+            }
+            if (gTime < gTarget) {
+                cnt++;
+                tgrp = grp;
+                long long oa = 0, ob = 0;
+                int dir = 0;
+                unsigned int code = 0;
+                bool have = false;
+                if (lane == 0) {
+                    const bool valid = cur ? bv1 : bv0;
+                    const unsigned long long key = valid ? (cur ? k1 : k0) : 0ull;
+                    if (valid) W = cur ? w1 : w0;
+                    // clear the entry the next update pass folds into
                     d.tileW[size_t(cur ^ 1) * size_t(d.ntiles) + size_t(it)] = 0u;
                     d.tileKey[size_t(cur ^ 1) * size_t(d.ntiles) + size_t(it)] = 0ull;
-                    float T = 0.f;
-                    if (key) {
-                        const size_t P = size_t(I.pitch);
-                        const float sp = sampleEdgeSpeed<S>(pick(d.h, cur) + I.base, pick(d.hu, cur) + I.base,
-                                                            pick(d.hv, cur) + I.base, P, int((key >> 16) & 0xffffull),
-                                                            int(key & 0xffffull), I.nx, I.ny);
-                        if (sp > 0.f) {
-                            smax = vmax(smax, sp);
-                            // the running maximum after this sample: a lower bound
-                            T = vmax(__uint_as_float(atomicMax(&G->speedBits, __float_as_uint(sp))), sp);
-                        }
-                    }
-                    if (!(W * kBoundMargin < T)) sCand[atomicAdd(&sNCand, 1)] = int(it - first) / int(gridDim.x);
+                    if (key) have = sampleEdge(I, it, int((key >> 16) & 0xffffull), int(key & 0xffffull), oa, ob, dir, code);
+                } else if (lane == 1 && pValid) {
+                    oa = pA;
+                    ob = pB;
+                    dir = pDir;
+                    have = true;  // code 0: already known
+                }
+                float sp = 0.f;
+                if (have)
+                    sp = vmax(0.f, edgeSpeedAt<S>(pick(d.h, cur), pick(d.hu, cur), pick(d.hv, cur), oa, ob, dir));
+                const float sp1 = __shfl_down_sync(0xffffffffu, sp, 1);
+                if (lane == 0) {
+                    samp = vmax(sp, sp1);
+                    if (sp > 0.f) bkey = umax64(bkey, speedKey(sp, code));
                 }
             }
         }
+        if (lane == 0) {
+            sSamp[wib] = samp;
+            sW[wib] = W;
+            sTileGrp[wib] = tgrp;
+        }
         __syncthreads();
-        // the candidates of this round, all warps on each
+        // 2. the largest exact speed the CTA sampled in the tile's group (the
+        // last pass's fastest edge among them) is a lower bound T
+        if (lane == 0 && tgrp >= 0) {
+            float T = 0.f;
+            for (int v = 0; v < nwb; v++)
+                if (sTileGrp[v] == tgrp) T = vmax(T, sSamp[v]);
+            if (!(W * kBoundMargin < T)) sCand[atomicAdd(&sNCand, 1)] = wib;
+        }
+        __syncthreads();
+        // 3. the candidates of this round, all warps on each
         const int ncand = sNCand;
         for (int c = 0; c < ncand; c++) {
-            const long long ct = first + (long long)gridDim.x * sCand[c];
+            const long long ct = (long long)((unsigned long long)(first + (long long)gridDim.x * sCand[c]) *
+                                             d.tileHashMul % (unsigned long long)d.ntiles);
             const TileInfo I = d.tileInfo[ct];
             GroupState *G = d.groups + I.group;
-            const int cur = G->cur;
+            const int cur = __ldg(&G->cur);
             const int xa = I.x0 + 4 * wib;
-            float m = 0.f;
-            if (xa < I.x1) {
-                const int xb = min(xa + 4, I.x1);
-                m = tileColumnsSpeed<S>(pick(d.h, cur) + I.base, pick(d.hu, cur) + I.base, pick(d.hv, cur) + I.base,
-                                        size_t(I.pitch), I, xa, xb, lane);
-            }
-            for (int o = 16; o > 0; o >>= 1) m = vmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-            if (lane == 0) sRed[wib] = m;
+            unsigned long long k = 0ull;
+            if (xa < I.x1)
+                k = tileColumnsSpeed<S>(pick(d.h, cur) + I.base, pick(d.hu, cur) + I.base, pick(d.hv, cur) + I.base,
+                                        size_t(I.pitch), I, ct, xa, min(xa + 4, I.x1), lane);
+            for (int o = 16; o > 0; o >>= 1) k = umax64(k, __shfl_xor_sync(0xffffffffu, k, o));
+            if (lane == 0) sKey[wib] = k;
             __syncthreads();
             if (threadIdx.x == 0) {
-                float mm = sRed[0];
-                for (int w = 1; w < nwb; w++) mm = vmax(mm, sRed[w]);
-                atomicMax(&G->speedBits, __float_as_uint(mm));
+                atomicAdd(&G->candidates, 1);
+                unsigned long long kk = sKey[0];
+                for (int w = 1; w < nwb; w++) kk = umax64(kk, sKey[w]);
+                if (kk) atomicMax(&G->maxEdge, kk);
             }
             __syncthreads();
         }
     }
     // combine the warps of the CTA per group, one arrival per group
-    float m = smax;
-    for (int o = 16; o > 0; o >>= 1) m = vmax(m, __shfl_xor_sync(0xffffffffu, m, o));
     if (lane == 0) {
-        sMax[wib] = m;
+        sKey[wib] = bkey;
         sGrp[wib] = grp;
         sCnt[wib] = cnt;
     }
@@ -240,15 +326,15 @@ template <int S> __global__ void __launch_bounds__(256, 4) speedBoundKernel(cons
         for (int w = 0; w < nwb; w++) {
             const int g = sGrp[w];
             if (g < 0 || sCnt[w] == 0) continue;
-            float mg = sMax[w];
+            unsigned long long kg = sKey[w];
             int cg = sCnt[w];
             for (int v = w + 1; v < nwb; v++)
                 if (sGrp[v] == g && sCnt[v] > 0) {
-                    mg = vmax(mg, sMax[v]);
+                    kg = umax64(kg, sKey[v]);
                     cg += sCnt[v];
                     sCnt[v] = 0;
                 }
-            boundTilesDone(d, d.groups + g, mg, cg);
+            boundTilesDone(d, d.groups + g, kg, cg);
         }
     }
 }

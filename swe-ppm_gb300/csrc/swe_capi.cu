@@ -521,6 +521,10 @@ int swe_gpu_domain_create(const swe_gpu_desc *desc, swe_gpu_domain **out) {
                     D->tiles.push_back(T);
                 }
         }
+        if (D->tiles.size() >= (size_t(1) << 19)) {  // edge codes hold 19 bits of tile id
+            D->bounded = false;
+            D->tiles.clear();
+        }
         int sms = 148;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, D->device);
         const long long want = ((long long)D->tiles.size() + 7) / 8;
@@ -602,6 +606,16 @@ int swe_gpu_domain_create(const swe_gpu_desc *desc, swe_gpu_domain **out) {
     D->dev.tileKey = D->dTileKey;
     D->dev.tileInfo = D->dTiles;
     D->dev.ntiles = int(D->tiles.size());
+    {  // a multiplier coprime to the tile count spreads neighbouring tiles over CTAs
+        const unsigned long long n = std::max<unsigned long long>(1, D->tiles.size());
+        unsigned long long m = 2654435761ull % n;
+        auto gcd = [](unsigned long long a, unsigned long long b) {
+            while (b) { const unsigned long long t = a % b; a = b; b = t; }
+            return a;
+        };
+        while (m == 0 || gcd(m, n) != 1) m++;
+        D->dev.tileHashMul = n == 1 ? 1 : m;
+    }
     *out = D;
     return SWE_GPU_OK;
 }
@@ -847,6 +861,22 @@ int swe_gpu_advance(swe_gpu_domain *dom, float t_end, int max_steps, int *steps_
     return SWE_GPU_OK;
 }
 
+int swe_gpu_speed_pass_stats(swe_gpu_domain *dom, int *tiles, int *evaluated) {
+    if (!dom) return fail(SWE_GPU_ERR_INVALID, "null domain handle");
+    CUDA_TRY(cudaSetDevice(dom->device));
+    std::vector<GroupState> g;
+    int rc = readGroups(dom, g);
+    if (rc) return rc;
+    int t = 0, e = 0;
+    for (const GroupState &s : g) {
+        t += s.tiles;
+        e += s.lastCandidates;
+    }
+    if (tiles) *tiles = dom->bounded ? t : 0;
+    if (evaluated) *evaluated = dom->bounded ? e : 0;
+    return SWE_GPU_OK;
+}
+
 int swe_gpu_launch_count(const swe_gpu_domain *dom, long long *count) {
     if (!dom || !count) return fail(SWE_GPU_ERR_INVALID, "null argument");
     *count = dom->launches;
@@ -984,7 +1014,7 @@ int noallocScratch(int device, NoAllocScratch **out) {
 __global__ void noallocSetupKernel(NoAllocScratch *s, BlockDesc b, int tileRows, int tileCols, int nunits) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i == 0) {
-        GroupState g;
+        GroupState g{};
         g.speedBits = 0u;
         g.arrived = 0u;
         g.units = nunits;
@@ -998,7 +1028,6 @@ __global__ void noallocSetupKernel(NoAllocScratch *s, BlockDesc b, int tileRows,
         g.cur = 0;
         g.status = 0;
         g.ghostsAhead = 0;
-        g.boundsValid[0] = g.boundsValid[1] = 0;
         s->group = g;
         s->block = b;
     }

@@ -61,9 +61,16 @@ struct WorkUnit {
 // where the reference's `while (t < checkpoint)` loop stops); the last CTA of
 // each pass (arrival counter) finishes the pass: dt after the speed pass,
 // time/steps/current buffer after the update pass.
-struct GroupState {
+struct __align__(128) GroupState {
+    // --- updated by atomics while a pass runs (a cache line of their own) ---
     unsigned int speedBits;  // max wave speed of the running step (float bits)
-    unsigned int arrived;    // segments of the running pass that have finished
+    unsigned int arrived;    // segments / tiles of the running pass that have finished
+    // the fastest edge found by the running bounded speed pass:
+    // (speed bits << 32) | edge code (bound tile << 13 | dir << 12 | lx << 6 | ly)
+    unsigned long long maxEdge;
+    int candidates;          // tiles evaluated edge by edge in the running pass
+    int hotPad[27];
+    // --- read by every CTA of a pass, written by the pass's last CTA ---
     int units;               // segments of the speed pass in this group
     int unitsUpd;            // segments of the update pass in this group
     int firstBlock;          // the group's first block (its dx, dy)
@@ -80,6 +87,12 @@ struct GroupState {
     // bounds and sample keys of parity p describe the state in buffer p
     int boundsValid[2];
     int tiles;               // bound tiles of the group's blocks
+    // the fastest edge of the last bounded speed pass as element offsets of
+    // its two cells (lower, upper) and direction (0: x-edge, 1: y-edge);
+    // its speed in the next state is a lower bound of the next maximum
+    long long prevA, prevB;
+    int prevDir, prevValid;
+    int lastCandidates;      // tiles the last bounded speed pass evaluated edge by edge
 };
 
 // Bound tile of the bounded speed pass: 32 x 32 interior cells of a block,
@@ -121,6 +134,7 @@ struct DomainDev {
     unsigned long long *tileKey;
     const TileInfo *tileInfo;
     int ntiles;
+    unsigned long long tileHashMul;  // coprime to ntiles: slot -> tile permutation
 };
 
 __device__ __forceinline__ float vmin(float a, float b) { return (b < a) ? b : a; }

@@ -63,9 +63,10 @@ __device__ __forceinline__ float timestepFromSpeed(float s, float dx, float dy, 
 /// buffer p of a double-buffered field without dynamic indexing of the kernel parameter
 __device__ __forceinline__ float *pick(float *const (&f)[2], int p) { return p ? f[1] : f[0]; }
 
-__device__ __forceinline__ bool groupActive(const GroupState *G) {
-    return *((volatile const float *)&G->time) < *((volatile const float *)&G->target);
-}
+/// the group still steps (time < target).  Time, target, the current buffer
+/// and dt change only in the last CTA of a pass, after every other CTA of the
+/// pass has read them, so the passes read them through the read-only path.
+__device__ __forceinline__ bool groupActive(const GroupState *G) { return __ldg(&G->time) < __ldg(&G->target); }
 
 /// per-cell quantities in x (normal momentum hu) and y (hv) direction:
 /// u = hu * (1/h), v = hv * (1/h), sqrt(h), sqrt(g) sqrt(h)
@@ -273,7 +274,7 @@ __global__ void __launch_bounds__(kMaxTileRows, 4) sweepKernel(const DomainDev d
         const BlockDesc B = d.blocks[wu.block];
         GroupState *G = d.groups + B.group;
         if (!groupActive(G)) continue;
-        const int cur = G->cur;
+        const int cur = __ldg(&G->cur);
         const float *__restrict__ H = pick(d.h, cur) + B.base;
         const float *__restrict__ HU = pick(d.hu, cur) + B.base;
         const float *__restrict__ HV = pick(d.hv, cur) + B.base;
@@ -288,7 +289,7 @@ __global__ void __launch_bounds__(kMaxTileRows, 4) sweepKernel(const DomainDev d
 
         float dtdx = 0.f, dtdy = 0.f;
         if (UPDATE) {
-            const float dt = G->dt;
+            const float dt = __ldg(&G->dt);
             dtdx = dt / B.dx;
             dtdy = (SEM == SEM_SPLIT) ? dtdx : dt / B.dy;
         }
@@ -441,7 +442,7 @@ template <int S> __global__ void __launch_bounds__(kMaxTileRows) speedSplitKerne
         const BlockDesc B = d.blocks[wu.block];
         GroupState *G = d.groups + B.group;
         if (!groupActive(G)) continue;
-        const int cur = G->cur;
+        const int cur = __ldg(&G->cur);
         const float *__restrict__ H = pick(d.h, cur) + B.base;
         const float *__restrict__ HU = pick(d.hu, cur) + B.base;
         const float *__restrict__ BT = d.b + B.base;

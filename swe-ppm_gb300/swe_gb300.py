@@ -42,7 +42,7 @@ EXPORTED = [
     "swe_gpu_advance", "swe_gpu_get_time", "swe_gpu_set_time", "swe_gpu_sync", "swe_gpu_status",
     "swe_gpu_get_stream", "swe_gpu_set_stream", "swe_gpu_last_error", "swe_gpu_version", "swe_gpu_solve_edges", "swe_gpu_step_block_noalloc",
     "swe_gpu_snapshot_slabs_async", "swe_gpu_snapshot_wait", "swe_gpu_alloc_pinned", "swe_gpu_free_pinned",
-    "swe_gpu_launch_count",
+    "swe_gpu_launch_count", "swe_gpu_speed_pass_stats",
     "swe_nc_open", "swe_nc_write_step", "swe_nc_write_step_slabs", "swe_nc_close",
     "swe_host_scenario_geometry", "swe_host_scenario_boundary", "swe_host_init_block", "swe_host_decompose",
 ]
@@ -96,6 +96,7 @@ def lib():
         L.swe_gpu_advance.argtypes = [vp, C.c_float, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_float)]
         L.swe_gpu_get_time.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_int)]
         L.swe_gpu_launch_count.argtypes = [vp, C.POINTER(C.c_longlong)]
+        L.swe_gpu_speed_pass_stats.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int)]
         L.swe_gpu_set_time.argtypes = [vp, C.c_float]
         L.swe_gpu_status.argtypes = [vp, C.POINTER(C.c_int)]
         L.swe_gpu_get_stream.argtypes = [vp, C.POINTER(vp)]
@@ -308,6 +309,12 @@ class Domain:
         n = C.c_longlong()
         _check(lib().swe_gpu_launch_count(self.handle, C.byref(n)))
         return n.value
+
+    def speed_pass_stats(self):
+        """(bound tiles, tiles the last bounded speed pass evaluated edge by edge)"""
+        t, e = C.c_int(), C.c_int()
+        _check(lib().swe_gpu_speed_pass_stats(self.handle, C.byref(t), C.byref(e)))
+        return t.value, e.value
 
     def set_time(self, t):
         _check(lib().swe_gpu_set_time(self.handle, float(t)))
