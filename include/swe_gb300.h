@@ -32,6 +32,7 @@ extern "C" {
 #define SWE_GPU_ERR_CUDA (-2)      /* CUDA runtime error */
 #define SWE_GPU_ERR_DEVICE (-3)    /* device-side status flag set (e.g. NaN wave speed) */
 #define SWE_GPU_ERR_NOMEM (-4)     /* device allocation failed */
+#define SWE_GPU_INCOMPLETE 1       /* not an error: an iteration budget ran out first */
 
 /* Riemann solvers.  The reference chooses at compile time with
  * WAVE_PROPAGATION_SOLVER (SConstruct:543-553, src/blocks/SWE_DimensionalSplittingMpi.hh:42-50):
@@ -94,6 +95,10 @@ typedef struct swe_gpu_desc {
                             unsplit step, CTA tiles): exact wave speeds only where
                             the previous update's speed bounds can reach the
                             maximum; 1 = every edge.  Both give the same dt. */
+    float lts_max_timestep; /* > 0: local time stepping with synchronisation
+                            intervals of this length (the drivers' -l; unsplit
+                            step only; advanced with swe_gpu_lts_advance) */
+    float duration;      /* simulated duration (local time stepping's last-step notice) */
 } swe_gpu_desc;
 
 int swe_gpu_domain_create(const swe_gpu_desc *desc, swe_gpu_domain **out);
@@ -157,6 +162,24 @@ int swe_gpu_step(swe_gpu_domain *dom, int nsteps);
  * graph; returns the executed steps and the float time reached */
 int swe_gpu_advance(swe_gpu_domain *dom, float t_end, int max_steps, int *steps_done, float *t_now);
 int swe_gpu_get_time(swe_gpu_domain *dom, float *t, int *steps);
+/* Local time stepping (domains created with lts_max_timestep > 0): runs
+ * synchronisation intervals of every block at its own power-of-two share of
+ * the interval, with time-interpolated ghost layers (src/blocks/SWE_Block.hh:311-562,
+ * src/examples/swe_mpi_overdecomp.cpp:266-343), until the interval start time
+ * t reaches t_end or max_iterations inner iterations ran.  The iterations are
+ * decided on the device and replayed from a captured graph; the host reads
+ * the control block once per batch.  Returns the finished intervals and t;
+ * SWE_GPU_INCOMPLETE when exactly max_iterations inner iterations ran first. */
+int swe_gpu_lts_advance(swe_gpu_domain *dom, float t_end, int max_iterations, int *intervals_done, float *t_now);
+/* Local time stepping counters: t, finished intervals, inner iterations and,
+ * when block_steps is not null, each block's number of steps (power-of-two
+ * divisor) in the last finished interval. */
+int swe_gpu_lts_state(swe_gpu_domain *dom, float *t, int *intervals, int *iterations, int *block_steps);
+/* Ghost-layer state machine of every block: ints[8k..8k+7] = the state of the
+ * LEFT, RIGHT, BOTTOM, TOP layers (0 done, 1 invalid, 2 interpolated, 3 in
+ * sync, 4 next), stepSize, stepSizeCounter, timestepCounter, last-timestep
+ * notice; border[4k..4k+3] = the neighbours' local times of the layers. */
+int swe_gpu_lts_blocks(swe_gpu_domain *dom, int *ints, float *border);
 /* Kernels this domain has enqueued so far (a replay of the captured step
  * graph counts each of its kernel nodes); no synchronisation. */
 int swe_gpu_launch_count(const swe_gpu_domain *dom, long long *count);

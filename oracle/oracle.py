@@ -67,6 +67,8 @@ def lib():
         L.oracle_domain_time.restype = C.c_double
         L.oracle_domain_time.argtypes = [C.c_void_p]
         L.oracle_domain_lts_interval.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+        L.oracle_domain_lts_iteration.argtypes = [C.c_void_p]
+        L.oracle_domain_lts_blocks.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         L.oracle_domain_block_max_timestep.restype = C.c_double
         L.oracle_domain_block_max_timestep.argtypes = [C.c_void_p, C.c_int]
         _lib = L
@@ -148,6 +150,18 @@ class Domain:
     @property
     def time(self):
         return lib().oracle_domain_time(self.h)
+
+    def lts_iteration(self):
+        """one inner local-time-stepping iteration (interval end included when it completes one)"""
+        return lib().oracle_domain_lts_iteration(self.h)
+
+    def lts_blocks(self):
+        """per block: int[8] (received[4], stepSize, stepSizeCounter, timestepCounter, notified), borderTimestep[4]"""
+        n = self.bx * self.by
+        ints = np.zeros((n, 8), dtype=np.int32)
+        border = np.zeros((n, 4), dtype=np.float64)
+        lib().oracle_domain_lts_blocks(self.h, _ptr(ints), _ptr(border))
+        return ints, border.astype(np.float32)
 
     def lts_interval(self, max_iterations=100000):
         steps = np.zeros(self.bx * self.by, dtype=np.int32)

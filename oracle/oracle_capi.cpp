@@ -210,6 +210,45 @@ int oracle_domain_lts_interval(void *h, int maxIterations, int *blockSteps) {
                 : ltsInterval(*H->d, H->t, maxIterations, blockSteps);
 }
 
+/// one inner iteration of local time stepping; when it completes the
+/// interval, the interval end too (t += maxTimestepLocal, counters reset).
+/// Returns 1 if the interval ended.
+int oracle_domain_lts_iteration(void *h) {
+    auto *H = static_cast<Handle *>(h);
+    auto run = [&](auto &D) {
+        const bool done = D.ltsIteration();
+        if (done) {
+            auto t = decltype(D.blocks[0].maxTimestepLocal)(H->t);
+            t += D.blocks[0].maxTimestepLocal;
+            H->t = double(t);
+            for (auto &B : D.blocks) B.resetStepSizeCounter();
+        }
+        return done ? 1 : 0;
+    };
+    return H->f ? run(*H->f) : run(*H->d);
+}
+
+/// local-time-stepping state of every block: ints[8k..8k+7] = received[4],
+/// stepSize, stepSizeCounter, timestepCounter, notified; border[4k..4k+3]
+int oracle_domain_lts_blocks(void *h, int *ints, double *border) {
+    auto *H = static_cast<Handle *>(h);
+    auto fill = [&](auto &D) {
+        for (size_t k = 0; k < D.blocks.size(); k++) {
+            const auto &B = D.blocks[k];
+            for (int s4 = 0; s4 < 4; s4++) {
+                ints[8 * k + s4] = B.receivedGhostlayer[s4];
+                border[4 * k + s4] = double(B.borderTimestep[s4]);
+            }
+            ints[8 * k + 4] = B.stepSize;
+            ints[8 * k + 5] = B.stepSizeCounter;
+            ints[8 * k + 6] = B.timestepCounter;
+            ints[8 * k + 7] = B.notifiedLastTimestep ? 1 : 0;
+        }
+        return 0;
+    };
+    return H->f ? fill(*H->f) : fill(*H->d);
+}
+
 /// the float dt the blocks last applied (maxTimestep of block k)
 double oracle_domain_block_max_timestep(void *h, int k) {
     auto *H = static_cast<Handle *>(h);

@@ -17,7 +17,7 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libswe_gb300.so")
 DRIVER = os.path.join(OUT, "swe_gb300")
 
-CUDA_SOURCES = ["csrc/swe_capi.cu", "csrc/swe_kernels_fh.cu", "csrc/swe_kernels_aug.cu"]
+CUDA_SOURCES = ["csrc/swe_capi.cu", "csrc/swe_kernels_fh.cu", "csrc/swe_kernels_aug.cu", "csrc/swe_lts.cu"]
 HOST_SOURCES = ["host/swe_host.cpp", "host/netcdf_writer.cpp"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-fmad=false", "-lineinfo", "-std=c++17",
               "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-I" + os.path.join(ROOT, "include")]

@@ -172,7 +172,7 @@ __device__ __forceinline__ void boundTilesDone(const DomainDev &d, GroupState *G
         }
         const BlockDesc &F = d.blocks[G->firstBlock];
         G->speed = s;
-        G->dt = timestepFromSpeed(s, F.dx, F.dy, SEM_UNSPLIT);
+        G->dt = groupTimestep(d, G, s, F.dx, F.dy);
         if (!(s == s)) G->status |= 1;
         G->lastCandidates = atomicAdd(&G->candidates, 0);
         G->candidates = 0;
@@ -223,6 +223,7 @@ template <int S> __global__ void __launch_bounds__(256, 4) speedBoundKernel(cons
             // group state (constant during the pass: read-only path, one L2
             // fetch per SM) and both parities of the tile entries at once
             const float gTime = __ldg(&G->time), gTarget = __ldg(&G->target);
+            const int gEnabled = __ldg(&G->enabled);
             const int cur = __ldg(&G->cur), bv0 = __ldg(&G->boundsValid[0]), bv1 = __ldg(&G->boundsValid[1]);
             const int pValid = __ldg(&G->prevValid), pDir = __ldg(&G->prevDir);
             const long long pA = __ldg(&G->prevA), pB = __ldg(&G->prevB);
@@ -244,7 +245,7 @@ template <int S> __global__ void __launch_bounds__(256, 4) speedBoundKernel(cons
                 k0 = __ldg(&d.tileKey[it]);
                 k1 = __ldg(&d.tileKey[size_t(d.ntiles) + size_t(it)]);
             }
-            if (gTime < gTarget) {
+            if (gTime < gTarget && gEnabled) {
                 cnt++;
                 tgrp = grp;
                 long long oa = 0, ob = 0;

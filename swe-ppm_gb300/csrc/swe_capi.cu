@@ -250,6 +250,14 @@ struct swe_gpu_domain {
     int gridB = 0;                    // CTAs of the bounded speed pass
     long long launches = 0;           // kernels enqueued (graph replays: per kernel node)
     long long graphKernels = 0;       // kernel nodes of the captured step graph
+    // local time stepping
+    bool lts = false;
+    LtsBlock *dLts = nullptr;
+    LtsControl *dLtsCtl = nullptr;
+    float *dRing[3] = {nullptr, nullptr, nullptr};
+    long long ringElems = 0;
+    cudaGraphExec_t ltsGraph = nullptr;
+    long long ltsGraphKernels = 0;
 };
 
 namespace {
@@ -300,6 +308,20 @@ int enqueueStep(swe_gpu_domain *D) {
     return enqueueUpdate(D);
 }
 
+/// one inner iteration of local time stepping (see swe_lts.cu)
+int enqueueLtsIteration(swe_gpu_domain *D) {
+    CUDA_TRY(launchLtsExchange(D->dev, D->maxPerimeter, D->stream));
+    CUDA_TRY(launchLtsCheck(D->dev, D->stream));
+    D->launches += 2;
+    int rc = enqueueSpeed(D);
+    if (rc) return rc;
+    rc = enqueueUpdate(D);
+    if (rc) return rc;
+    CUDA_TRY(launchLtsDone(D->dev, D->stream));
+    D->launches++;
+    return SWE_GPU_OK;
+}
+
 int readGroups(swe_gpu_domain *D, std::vector<GroupState> &g) {
     g.resize(D->ngroups);
     CUDA_TRY(cudaStreamSynchronize(D->stream));
@@ -316,6 +338,10 @@ int setTargets(swe_gpu_domain *D, float target) {
 
 void freeDomain(swe_gpu_domain *D) {
     if (D->graph) cudaGraphExecDestroy(D->graph);
+    if (D->ltsGraph) cudaGraphExecDestroy(D->ltsGraph);
+    cudaFree(D->dLts);
+    cudaFree(D->dLtsCtl);
+    for (int f = 0; f < 3; f++) cudaFree(D->dRing[f]);
     if (D->snapEvent) cudaEventDestroy(D->snapEvent);
     for (int i = 0; i < 2; i++) {
         cudaFree(D->h[i]);
@@ -365,6 +391,8 @@ int swe_gpu_domain_create(const swe_gpu_desc *desc, swe_gpu_domain **out) {
         return fail(SWE_GPU_ERR_INVALID, "unknown semantics %d", desc->semantics);
     if (desc->semantics == SWE_SEMANTICS_SPLIT && bx * by != 1)
         return fail(SWE_GPU_ERR_INVALID, "the split step is defined for a single block");
+    if (desc->lts_max_timestep > 0.f && desc->semantics != SWE_SEMANTICS_UNSPLIT)
+        return fail(SWE_GPU_ERR_INVALID, "local time stepping is defined for the unsplit step");
     for (int i = 0; i < 4; i++)
         if (desc->boundary[i] < SWE_OUTFLOW || desc->boundary[i] > SWE_PASSIVE)
             return fail(SWE_GPU_ERR_INVALID, "unknown boundary type %d", desc->boundary[i]);
@@ -379,6 +407,7 @@ int swe_gpu_domain_create(const swe_gpu_desc *desc, swe_gpu_domain **out) {
 
     auto *D = new swe_gpu_domain();
     D->device = desc->device;
+    D->lts = desc->lts_max_timestep > 0.f;
     D->solver = desc->solver;
     D->semantics = desc->semantics;
     D->splitDtMode = desc->split_dt_mode;
@@ -411,8 +440,10 @@ int swe_gpu_domain_create(const swe_gpu_desc *desc, swe_gpu_domain **out) {
         B.nx = desc->nx_cols[px];
         B.ny = desc->ny_rows[py];
         B.pitch = ((B.ny + 2 + kColPad) + 31) / 32 * 32;
-        B.group = 0;
+        B.group = D->lts ? k : 0;  // local time stepping: every block its own dt group
         B.base = (long long)elems + kColPad;
+        B.ring = D->ringElems;
+        D->ringElems += 2LL * (B.nx + B.ny);
         B.dx = desc->dx;
         B.dy = desc->dy;
         const int nb[4] = {px > 0 ? k - by : -1, px < bx - 1 ? k + by : -1, py > 0 ? k - 1 : -1,
@@ -495,7 +526,8 @@ int swe_gpu_domain_create(const swe_gpu_desc *desc, swe_gpu_domain **out) {
         auto tilesX = [&](int k) { return (D->blocks[k].nx + kBoundTile - 1) / kBoundTile; };
         auto ghostSide = [&](const BlockDesc &B, int side, int nbTile) {
             const int type = B.bnd[side];
-            if (type == CONNECT_WITHIN_RANK) return nbTile;
+            // local time stepping time-interpolates these ghosts: no bound
+            if (type == CONNECT_WITHIN_RANK) return D->lts ? kNbrUnbounded : nbTile;
             return (type == OUTFLOW || type == WALL) ? kNbrSelf : kNbrUnbounded;
         };
         for (int k = 0; k < int(D->blocks.size()); k++) {
@@ -530,15 +562,18 @@ int swe_gpu_domain_create(const swe_gpu_desc *desc, swe_gpu_domain **out) {
         const long long want = ((long long)D->tiles.size() + 7) / 8;
         D->gridB = int(std::max(1LL, std::min(want, (long long)sms * std::max(1, occupancyBound(D->solver)))));
     }
-    GroupState g0{};
-    g0.units = int(D->units.size());
-    g0.unitsUpd = int(D->unitsU.size());
-    g0.tiles = int(D->tiles.size());
-    g0.firstBlock = 0;
-    g0.target = INFINITY;
-    g0.dt = 0.f;
-    D->groupsInit.assign(1, g0);
-    D->ngroups = 1;
+    // dt groups: the whole domain, or (local time stepping) one per block
+    D->ngroups = D->lts ? int(D->blocks.size()) : 1;
+    {
+        GroupState g0{};
+        g0.target = INFINITY;
+        g0.enabled = D->lts ? 0 : 1;
+        D->groupsInit.assign(D->ngroups, g0);
+        for (int g = 0; g < D->ngroups; g++) D->groupsInit[g].firstBlock = D->lts ? g : 0;
+        for (const WorkUnit &u : D->units) D->groupsInit[D->blocks[u.block].group].units++;
+        for (const WorkUnit &u : D->unitsU) D->groupsInit[D->blocks[u.block].group].unitsUpd++;
+        for (const TileInfo &t : D->tiles) D->groupsInit[t.group].tiles++;
+    }
 
     bool ok = true;
     const size_t bytes = elems * sizeof(float);
@@ -553,6 +588,12 @@ int swe_gpu_domain_create(const swe_gpu_desc *desc, swe_gpu_domain **out) {
     ok = ok && cudaMalloc(&D->dUnitsU, sizeof(WorkUnit) * D->unitsU.size()) == cudaSuccess;
     ok = ok && cudaMalloc(&D->dCtaSegU, sizeof(int) * D->ctaSegU.size()) == cudaSuccess;
     ok = ok && cudaMalloc(&D->dGroups, sizeof(GroupState) * D->ngroups) == cudaSuccess;
+    if (D->lts) {
+        ok = ok && cudaMalloc(&D->dLts, sizeof(LtsBlock) * D->blocks.size()) == cudaSuccess;
+        ok = ok && cudaMalloc(&D->dLtsCtl, sizeof(LtsControl)) == cudaSuccess;
+        for (int f = 0; f < 3 && ok; f++)
+            ok = cudaMalloc(&D->dRing[f], sizeof(float) * std::max(1LL, D->ringElems)) == cudaSuccess;
+    }
     if (D->bounded) {
         ok = ok && cudaMalloc(&D->dTiles, sizeof(TileInfo) * D->tiles.size()) == cudaSuccess;
         ok = ok && cudaMalloc(&D->dTileW, sizeof(unsigned int) * 2 * D->tiles.size()) == cudaSuccess;
@@ -575,6 +616,22 @@ int swe_gpu_domain_create(const swe_gpu_desc *desc, swe_gpu_domain **out) {
     cudaMemcpyAsync(D->dUnitsU, D->unitsU.data(), sizeof(WorkUnit) * D->unitsU.size(), cudaMemcpyHostToDevice, D->stream);
     cudaMemcpyAsync(D->dCtaSegU, D->ctaSegU.data(), sizeof(int) * D->ctaSegU.size(), cudaMemcpyHostToDevice, D->stream);
     cudaMemcpyAsync(D->dGroups, D->groupsInit.data(), sizeof(GroupState) * D->ngroups, cudaMemcpyHostToDevice, D->stream);
+    std::vector<LtsBlock> ltsInit;
+    LtsControl ctlInit{};
+    if (D->lts) {
+        LtsBlock l0{};
+        for (int s4 = 0; s4 < 4; s4++) l0.received[s4] = GL_NEXT;
+        ltsInit.assign(D->blocks.size(), l0);
+        ctlInit.t = 0.f;
+        ctlInit.target = 0.f;  // nothing runs before swe_gpu_lts_advance
+        ctlInit.maxTimestepLocal = desc->lts_max_timestep;
+        ctlInit.duration = desc->duration;
+        ctlInit.maxDivisor = 1024;  // src/blocks/SWE_Block.hh:221
+        cudaMemcpyAsync(D->dLts, ltsInit.data(), sizeof(LtsBlock) * ltsInit.size(), cudaMemcpyHostToDevice, D->stream);
+        cudaMemcpyAsync(D->dLtsCtl, &ctlInit, sizeof(LtsControl), cudaMemcpyHostToDevice, D->stream);
+        for (int f = 0; f < 3; f++)
+            cudaMemsetAsync(D->dRing[f], 0, sizeof(float) * std::max(1LL, D->ringElems), D->stream);
+    }
     if (D->bounded) {
         cudaMemcpyAsync(D->dTiles, D->tiles.data(), sizeof(TileInfo) * D->tiles.size(), cudaMemcpyHostToDevice,
                         D->stream);
@@ -602,6 +659,9 @@ int swe_gpu_domain_create(const swe_gpu_desc *desc, swe_gpu_domain **out) {
     D->dev.splitDtMode = D->splitDtMode;
     D->dev.variant = D->variant;
     D->dev.tileRows = D->tileRows;
+    D->dev.lts = D->dLts;
+    D->dev.ltsCtl = D->dLtsCtl;
+    for (int f = 0; f < 3; f++) D->dev.ring[f] = D->dRing[f];
     D->dev.tileW = D->dTileW;
     D->dev.tileKey = D->dTileKey;
     D->dev.tileInfo = D->dTiles;
@@ -770,6 +830,7 @@ int swe_gpu_exchange_bathymetry(swe_gpu_domain *dom) {
 }
 
 int swe_gpu_set_ghost_layer(swe_gpu_domain *dom) {
+    if (dom && dom->lts) return fail(SWE_GPU_ERR_INVALID, "local-time-stepping domain: use swe_gpu_lts_advance");
     if (!dom) return fail(SWE_GPU_ERR_INVALID, "null domain handle");
     CUDA_TRY(cudaSetDevice(dom->device));
     int rc = enqueueGhost(dom, 0);
@@ -778,6 +839,7 @@ int swe_gpu_set_ghost_layer(swe_gpu_domain *dom) {
 }
 
 int swe_gpu_compute_fluxes(swe_gpu_domain *dom) {
+    if (dom && dom->lts) return fail(SWE_GPU_ERR_INVALID, "local-time-stepping domain: use swe_gpu_lts_advance");
     if (!dom) return fail(SWE_GPU_ERR_INVALID, "null domain handle");
     CUDA_TRY(cudaSetDevice(dom->device));
     return enqueueSpeed(dom);
@@ -785,6 +847,7 @@ int swe_gpu_compute_fluxes(swe_gpu_domain *dom) {
 
 int swe_gpu_update_unknowns(swe_gpu_domain *dom, float dt) {
     (void)dt;
+    if (dom && dom->lts) return fail(SWE_GPU_ERR_INVALID, "local-time-stepping domain: use swe_gpu_lts_advance");
     if (!dom) return fail(SWE_GPU_ERR_INVALID, "null domain handle");
     CUDA_TRY(cudaSetDevice(dom->device));
     return enqueueUpdate(dom);
@@ -801,6 +864,7 @@ int swe_gpu_get_max_timestep(swe_gpu_domain *dom, float *dt) {
 }
 
 int swe_gpu_step(swe_gpu_domain *dom, int nsteps) {
+    if (dom && dom->lts) return fail(SWE_GPU_ERR_INVALID, "local-time-stepping domain: use swe_gpu_lts_advance");
     if (!dom || nsteps < 0) return fail(SWE_GPU_ERR_INVALID, "bad argument");
     CUDA_TRY(cudaSetDevice(dom->device));
     for (int i = 0; i < nsteps; i++) {
@@ -812,6 +876,7 @@ int swe_gpu_step(swe_gpu_domain *dom, int nsteps) {
 
 int swe_gpu_advance(swe_gpu_domain *dom, float t_end, int max_steps, int *steps_done, float *t_now) {
     if (!dom || max_steps < 0) return fail(SWE_GPU_ERR_INVALID, "bad argument");
+    if (dom->lts) return fail(SWE_GPU_ERR_INVALID, "local-time-stepping domain: use swe_gpu_lts_advance");
     CUDA_TRY(cudaSetDevice(dom->device));
     const int batch = 16;
     if (!dom->graph) {  // capture `batch` steps once; replays are identical
@@ -858,6 +923,93 @@ int swe_gpu_advance(swe_gpu_domain *dom, float t_end, int max_steps, int *steps_
     if (steps_done) *steps_done = done;
     if (t_now) *t_now = g[0].time;
     if (g[0].status) return fail(SWE_GPU_ERR_DEVICE, "device status 0x%x (NaN wave speed)", g[0].status);
+    return SWE_GPU_OK;
+}
+
+int swe_gpu_lts_advance(swe_gpu_domain *dom, float t_end, int max_iterations, int *intervals_done, float *t_now) {
+    if (!dom || max_iterations < 0) return fail(SWE_GPU_ERR_INVALID, "bad argument");
+    if (!dom->lts) return fail(SWE_GPU_ERR_INVALID, "not a local-time-stepping domain");
+    CUDA_TRY(cudaSetDevice(dom->device));
+    const int batch = 8;  // inner iterations per graph replay
+    if (!dom->ltsGraph) {
+        cudaGraph_t g;
+        CUDA_TRY(cudaStreamBeginCapture(dom->stream, cudaStreamCaptureModeThreadLocal));
+        int rc = SWE_GPU_OK;
+        const long long before = dom->launches;
+        for (int i = 0; i < batch && rc == SWE_GPU_OK; i++) rc = enqueueLtsIteration(dom);
+        cudaError_t e = cudaStreamEndCapture(dom->stream, &g);
+        dom->ltsGraphKernels = dom->launches - before;
+        dom->launches = before;
+        if (rc) return rc;
+        if (e != cudaSuccess) return fail(SWE_GPU_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&dom->ltsGraph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return fail(SWE_GPU_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+    }
+    LtsControl c{};
+    CUDA_TRY(cudaMemcpyAsync(&c, dom->dLtsCtl, sizeof(LtsControl), cudaMemcpyDeviceToHost, dom->stream));
+    CUDA_TRY(cudaStreamSynchronize(dom->stream));
+    const int startIntervals = c.intervals, startIterations = c.iterations;
+    const int limit = int(std::min<long long>(INT32_MAX, (long long)c.iterations + max_iterations));
+    CUDA_TRY(cudaMemcpyAsync(&dom->dLtsCtl->target, &t_end, sizeof(float), cudaMemcpyHostToDevice, dom->stream));
+    CUDA_TRY(cudaMemcpyAsync(&dom->dLtsCtl->iterLimit, &limit, sizeof(int), cudaMemcpyHostToDevice, dom->stream));
+    while (c.t < t_end && c.iterations < limit) {
+        CUDA_TRY(cudaGraphLaunch(dom->ltsGraph, dom->stream));
+        dom->launches += dom->ltsGraphKernels;
+        CUDA_TRY(cudaMemcpyAsync(&c, dom->dLtsCtl, sizeof(LtsControl), cudaMemcpyDeviceToHost, dom->stream));
+        CUDA_TRY(cudaStreamSynchronize(dom->stream));
+    }
+    // stop: no kernel runs until the next call sets a new target
+    const float stop = -INFINITY;
+    CUDA_TRY(cudaMemcpyAsync(&dom->dLtsCtl->target, &stop, sizeof(float), cudaMemcpyHostToDevice, dom->stream));
+    CUDA_TRY(cudaStreamSynchronize(dom->stream));
+    if (intervals_done) *intervals_done = c.intervals - startIntervals;
+    if (t_now) *t_now = c.t;
+    std::vector<GroupState> g;
+    int rc = readGroups(dom, g);
+    if (rc) return rc;
+    int status = 0;
+    for (const GroupState &s : g) status |= s.status;
+    if (status) return fail(SWE_GPU_ERR_DEVICE, "device status 0x%x", status);
+    if (c.t < t_end && c.iterations - startIterations >= max_iterations)
+        return SWE_GPU_INCOMPLETE;  // the iteration budget ran out first
+    return SWE_GPU_OK;
+}
+
+int swe_gpu_lts_state(swe_gpu_domain *dom, float *t, int *intervals, int *iterations, int *block_steps) {
+    if (!dom) return fail(SWE_GPU_ERR_INVALID, "null domain handle");
+    if (!dom->lts) return fail(SWE_GPU_ERR_INVALID, "not a local-time-stepping domain");
+    CUDA_TRY(cudaSetDevice(dom->device));
+    LtsControl c{};
+    std::vector<LtsBlock> L(dom->blocks.size());
+    CUDA_TRY(cudaMemcpyAsync(&c, dom->dLtsCtl, sizeof(LtsControl), cudaMemcpyDeviceToHost, dom->stream));
+    CUDA_TRY(cudaMemcpyAsync(L.data(), dom->dLts, sizeof(LtsBlock) * L.size(), cudaMemcpyDeviceToHost, dom->stream));
+    CUDA_TRY(cudaStreamSynchronize(dom->stream));
+    if (t) *t = c.t;
+    if (intervals) *intervals = c.intervals;
+    if (iterations) *iterations = c.iterations;
+    if (block_steps)
+        for (size_t k = 0; k < L.size(); k++) block_steps[k] = L[k].lastStepSize;
+    return SWE_GPU_OK;
+}
+
+int swe_gpu_lts_blocks(swe_gpu_domain *dom, int *ints, float *border) {
+    if (!dom || !ints || !border) return fail(SWE_GPU_ERR_INVALID, "null argument");
+    if (!dom->lts) return fail(SWE_GPU_ERR_INVALID, "not a local-time-stepping domain");
+    CUDA_TRY(cudaSetDevice(dom->device));
+    std::vector<LtsBlock> L(dom->blocks.size());
+    CUDA_TRY(cudaMemcpyAsync(L.data(), dom->dLts, sizeof(LtsBlock) * L.size(), cudaMemcpyDeviceToHost, dom->stream));
+    CUDA_TRY(cudaStreamSynchronize(dom->stream));
+    for (size_t k = 0; k < L.size(); k++) {
+        for (int s4 = 0; s4 < 4; s4++) {
+            ints[8 * k + s4] = L[k].received[s4];
+            border[4 * k + s4] = L[k].borderTimestep[s4];
+        }
+        ints[8 * k + 4] = L[k].stepSize;
+        ints[8 * k + 5] = L[k].stepSizeCounter;
+        ints[8 * k + 6] = L[k].timestepCounter;
+        ints[8 * k + 7] = L[k].notified;
+    }
     return SWE_GPU_OK;
 }
 
@@ -1015,6 +1167,7 @@ __global__ void noallocSetupKernel(NoAllocScratch *s, BlockDesc b, int tileRows,
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i == 0) {
         GroupState g{};
+        g.enabled = 1;
         g.speedBits = 0u;
         g.arrived = 0u;
         g.units = nunits;

@@ -34,6 +34,8 @@ enum SolverId { SOLVER_FWAVE = 1, SOLVER_AUGRIE = 2, SOLVER_HYBRID = 3, SOLVER_H
 enum Semantics { SEM_UNSPLIT = 0, SEM_SPLIT = 1 };
 enum BoundaryType { OUTFLOW = 0, WALL = 1, INFLOW = 2, CONNECT = 3, CONNECT_WITHIN_RANK = 4, PASSIVE = 5 };
 enum SplitDtMode { SPLIT_DT_MAX = 0, SPLIT_DT_LAST_EDGE = 1 };
+// states of a received ghost layer under local time stepping (src/blocks/SWE_Block.hh)
+enum GhostlayerState { GL_DONE = 0, GL_UNVALID = 1, GL_INTER = 2, GL_SYNC = 3, GL_NEXT = 4 };
 /// thread mapping of the sweep kernels: warp strips of 4, 2 or 1 rows per
 /// lane, or CTA tiles
 enum KernelVariant { VARIANT_WARP = 0, VARIANT_TILE = 1, VARIANT_WARP2 = 2, VARIANT_WARP1 = 3 };
@@ -49,6 +51,30 @@ struct BlockDesc {
     long long stage;  // offset of the block in the contiguous host-order layout
     int tileBase;     // first bound tile of the block (bounded speed pass)
     int tilesY;       // bound tiles per column of tiles: ceil(ny / 32)
+    long long ring;   // local time stepping: offset of the block's receive ring
+                      // (LEFT ny, RIGHT ny, BOTTOM nx, TOP nx values per field)
+};
+
+// Per-block state of local time stepping (src/blocks/SWE_Block.hh:214-229).
+struct LtsBlock {
+    int received[4];          // GhostlayerState per side
+    float borderTimestep[4];  // the neighbour's total local time when its layer was received
+    int stepSize, stepSizeCounter, timestepCounter, notified;
+    int lastStepSize;         // stepSize of the last finished interval
+    int pad[3];
+};
+
+// Interval control of local time stepping (the drivers' outer loop,
+// src/examples/swe_mpi_overdecomp.cpp:308-343).
+struct LtsControl {
+    float t;                  // time at the start of the running interval
+    float target;             // intervals run while t < target
+    float maxTimestepLocal;   // length of a synchronisation interval (-l)
+    float duration;           // simulated duration (last-timestep detection)
+    int maxDivisor;           // finest subdivision of an interval
+    int intervals;            // finished intervals
+    int iterations;           // inner iterations run
+    int iterLimit;            // inner iterations run while iterations < iterLimit
 };
 
 // work unit of the sweep kernels: one block, rows [y0, y0+TY) x columns [x0, x1)
@@ -87,6 +113,7 @@ struct __align__(128) GroupState {
     // bounds and sample keys of parity p describe the state in buffer p
     int boundsValid[2];
     int tiles;               // bound tiles of the group's blocks
+    int enabled;             // 0: the group sits this step out (local time stepping)
     // the fastest edge of the last bounded speed pass as element offsets of
     // its two cells (lower, upper) and direction (0: x-edge, 1: y-edge);
     // its speed in the next state is a lower bound of the next maximum
@@ -135,6 +162,10 @@ struct DomainDev {
     const TileInfo *tileInfo;
     int ntiles;
     unsigned long long tileHashMul;  // coprime to ntiles: slot -> tile permutation
+    // local time stepping (null without): one group per block
+    LtsBlock *lts;
+    LtsControl *ltsCtl;
+    float *ring[3];                  // receive rings of h, hu, hv
 };
 
 __device__ __forceinline__ float vmin(float a, float b) { return (b < a) ? b : a; }

@@ -21,6 +21,12 @@ cudaError_t launchUpdateAug(const DomainDev &d, int nunits, int threads, cudaStr
 cudaError_t launchSpeedBound(const DomainDev &d, int grid, cudaStream_t s);
 int occupancyBound(int solver);
 
+// local time stepping: exchange, ghost-layer check and interval end of one
+// inner iteration (swe_lts.cu)
+cudaError_t launchLtsExchange(const DomainDev &d, int maxPerimeter, cudaStream_t s);
+cudaError_t launchLtsCheck(const DomainDev &d, cudaStream_t s);
+cudaError_t launchLtsDone(const DomainDev &d, cudaStream_t s);
+
 // resident CTAs per SM of the step kernels (the smaller of the two passes)
 int occupancyFH(int variant, int solver, int sem, bool update, int threads);
 int occupancyAug(int variant, int solver, int sem, bool update, int threads);

@@ -66,7 +66,41 @@ __device__ __forceinline__ float *pick(float *const (&f)[2], int p) { return p ?
 /// the group still steps (time < target).  Time, target, the current buffer
 /// and dt change only in the last CTA of a pass, after every other CTA of the
 /// pass has read them, so the passes read them through the read-only path.
-__device__ __forceinline__ bool groupActive(const GroupState *G) { return __ldg(&G->time) < __ldg(&G->target); }
+__device__ __forceinline__ bool groupActive(const GroupState *G) {
+    return __ldg(&G->time) < __ldg(&G->target) && __ldg(&G->enabled);
+}
+
+/// total local time of a block (SWE_Block::getTotalLocalTimestep,
+/// src/blocks/SWE_Block.hh:557-562)
+__device__ __forceinline__ float ltsTotalLocal(const LtsBlock &L, const LtsControl &C) {
+    return float(C.maxTimestepLocal * L.timestepCounter) +
+           (L.stepSize > 0 ? float(C.maxTimestepLocal * L.stepSizeCounter) / float(L.stepSize) : 0.f);
+}
+
+/// the block's time step rounded to Tsync / 2^k at the start of an interval
+/// (SWE_Block::getRoundTimestep, src/blocks/SWE_Block.hh:536-555), same float
+/// and double operations as the CPU restatement
+__device__ __forceinline__ float ltsRoundTimestep(LtsBlock &L, const LtsControl &C, float timestep) {
+    if (L.stepSizeCounter <= 0) {
+        if (timestep > C.maxTimestepLocal) timestep = C.maxTimestepLocal;
+        if (timestep < C.maxTimestepLocal / float(C.maxDivisor)) timestep = C.maxTimestepLocal / float(C.maxDivisor);
+        const float logT = logf(timestep);
+        const double ln2 = 0x1.62e42fefa39efp-1;  // ln 2, correctly rounded
+        const double e = ceil(double(logT) / ln2);
+        int divisor = int(ldexp(1.0, -int(e)));
+        if (1.f / float(divisor) > timestep) divisor *= 2;
+        L.stepSize = divisor > C.maxDivisor ? C.maxDivisor : divisor;
+    }
+    return C.maxTimestepLocal / float(L.stepSize);
+}
+
+/// maxTimestep of a group from its max wave speed; under local time stepping
+/// the group is one block and the step is rounded to its interval's grid
+__device__ __forceinline__ float groupTimestep(const DomainDev &d, const GroupState *G, float s, float dx, float dy) {
+    float dt = timestepFromSpeed(s, dx, dy, d.semantics);
+    if (d.lts) dt = ltsRoundTimestep(d.lts[G - d.groups], *d.ltsCtl, dt);
+    return dt;
+}
 
 /// per-cell quantities in x (normal momentum hu) and y (hv) direction:
 /// u = hu * (1/h), v = hv * (1/h), sqrt(h), sqrt(g) sqrt(h)
@@ -107,7 +141,7 @@ __device__ __forceinline__ void segmentDone(const DomainDev &d, GroupState *G, f
             G->time = G->time + G->dt;
             G->steps = G->steps + 1;
             G->cur = cur ^ 1;
-            G->ghostsAhead = 1;
+            G->ghostsAhead = d.lts ? 0 : 1;  // local time stepping rebuilds the ring itself
             // speed bounds now describe the output buffer
             G->boundsValid[cur] = 0;
             G->boundsValid[cur ^ 1] = d.tileW ? 1 : 0;
@@ -145,7 +179,7 @@ __device__ __forceinline__ void segmentDone(const DomainDev &d, GroupState *G, f
                 s = vmax(0.f, s);
             }
             G->speed = s;
-            G->dt = timestepFromSpeed(s, F.dx, F.dy, d.semantics);
+            G->dt = groupTimestep(d, G, s, F.dx, F.dy);
             if (!(s == s)) G->status |= 1;  // NaN wave speed
             G->speedBits = 0u;
             G->arrived = 0u;
@@ -210,7 +244,9 @@ static __device__ __noinline__ void pushGhosts(const DomainDev &d, const BlockDe
     for (int side = 0; side < 4; side++) {
         const bool on = side == 0 ? x == 1 : side == 1 ? x == B.nx : side == 2 ? y == 1 : y == B.ny;
         if (!on) continue;
-        const int type = B.bnd[side];
+        // local time stepping rebuilds the ghost ring every iteration from the
+        // ring kept in the new buffer (the reference's single array keeps it)
+        const int type = d.lts ? PASSIVE : B.bnd[side];
         const int gx = side == 0 ? 0 : side == 1 ? B.nx + 1 : x;
         const int gy = side == 2 ? 0 : side == 3 ? B.ny + 1 : y;
         const size_t g = size_t(B.base) + size_t(gx) * P + size_t(gy);
@@ -233,13 +269,19 @@ static __device__ __noinline__ void pushGhosts(const DomainDev &d, const BlockDe
         }
     }
     // corners come from the diagonal interior cell whatever the boundary type
+    // (local time stepping: kept, they are set at the start of each iteration)
     if (edgeX && edgeY) {
         for (int cxi = 0; cxi < 2; cxi++)
             for (int cyi = 0; cyi < 2; cyi++) {
                 const int sx = cxi ? B.nx : 1, sy = cyi ? B.ny : 1;
                 if (sx != x || sy != y) continue;
                 const size_t g = size_t(B.base) + size_t(cxi ? B.nx + 1 : 0) * P + size_t(cyi ? B.ny + 1 : 0);
-                HO[g] = h; HUO[g] = hu; HVO[g] = hv;
+                if (d.lts) {
+                    const float *HI = pick(d.h, outBuf ^ 1), *HUI = pick(d.hu, outBuf ^ 1), *HVI = pick(d.hv, outBuf ^ 1);
+                    HO[g] = HI[g]; HUO[g] = HUI[g]; HVO[g] = HVI[g];
+                } else {
+                    HO[g] = h; HUO[g] = hu; HVO[g] = hv;
+                }
             }
     }
 }

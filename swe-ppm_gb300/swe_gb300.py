@@ -42,7 +42,7 @@ EXPORTED = [
     "swe_gpu_advance", "swe_gpu_get_time", "swe_gpu_set_time", "swe_gpu_sync", "swe_gpu_status",
     "swe_gpu_get_stream", "swe_gpu_set_stream", "swe_gpu_last_error", "swe_gpu_version", "swe_gpu_solve_edges", "swe_gpu_step_block_noalloc",
     "swe_gpu_snapshot_slabs_async", "swe_gpu_snapshot_wait", "swe_gpu_alloc_pinned", "swe_gpu_free_pinned",
-    "swe_gpu_launch_count", "swe_gpu_speed_pass_stats",
+    "swe_gpu_launch_count", "swe_gpu_speed_pass_stats", "swe_gpu_lts_advance", "swe_gpu_lts_state", "swe_gpu_lts_blocks",
     "swe_nc_open", "swe_nc_write_step", "swe_nc_write_step_slabs", "swe_nc_close",
     "swe_host_scenario_geometry", "swe_host_scenario_boundary", "swe_host_init_block", "swe_host_decompose",
 ]
@@ -57,7 +57,8 @@ class Desc(C.Structure):
                 ("ny_rows", C.POINTER(C.c_int)), ("dx", C.c_float), ("dy", C.c_float),
                 ("boundary", C.c_int * 4), ("solver", C.c_int), ("semantics", C.c_int),
                 ("split_dt_mode", C.c_int), ("tile_rows", C.c_int), ("tile_cols", C.c_int), ("device", C.c_int),
-                ("kernel_variant", C.c_int), ("speed_pass", C.c_int)]
+                ("kernel_variant", C.c_int), ("speed_pass", C.c_int), ("lts_max_timestep", C.c_float),
+                ("duration", C.c_float)]
 
 
 _lib = None
@@ -97,6 +98,9 @@ def lib():
         L.swe_gpu_get_time.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_int)]
         L.swe_gpu_launch_count.argtypes = [vp, C.POINTER(C.c_longlong)]
         L.swe_gpu_speed_pass_stats.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        L.swe_gpu_lts_advance.argtypes = [vp, C.c_float, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_float)]
+        L.swe_gpu_lts_state.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_int), C.POINTER(C.c_int), vp]
+        L.swe_gpu_lts_blocks.argtypes = [vp, vp, vp]
         L.swe_gpu_set_time.argtypes = [vp, C.c_float]
         L.swe_gpu_status.argtypes = [vp, C.POINTER(C.c_int)]
         L.swe_gpu_get_stream.argtypes = [vp, C.POINTER(vp)]
@@ -205,7 +209,8 @@ class Domain:
     """Blocks of one simulation on the GPU (global time step)."""
 
     def __init__(self, nx_cols, ny_rows, dx, dy, boundary=(OUTFLOW,) * 4, solver=HLLE, semantics=UNSPLIT,
-                 split_dt_mode=SPLIT_DT_MAX, tile_rows=0, tile_cols=0, device=0, kernel_variant=0, speed_pass=0):
+                 split_dt_mode=SPLIT_DT_MAX, tile_rows=0, tile_cols=0, device=0, kernel_variant=0, speed_pass=0,
+                 lts_max_timestep=0.0, duration=0.0):
         self.nx_cols = [int(v) for v in nx_cols]
         self.ny_rows = [int(v) for v in ny_rows]
         self.bx, self.by = len(self.nx_cols), len(self.ny_rows)
@@ -222,6 +227,7 @@ class Domain:
         d.tile_rows, d.tile_cols, d.device = int(tile_rows), int(tile_cols), int(device)
         d.kernel_variant = int(kernel_variant)
         d.speed_pass = int(speed_pass)
+        d.lts_max_timestep, d.duration = float(lts_max_timestep), float(duration)
         self.handle = C.c_void_p()
         _check(lib().swe_gpu_domain_create(C.byref(d), C.byref(self.handle)))
         self.shapes = [(self.nx_cols[k // self.by], self.ny_rows[k % self.by]) for k in range(self.bx * self.by)]
@@ -309,6 +315,31 @@ class Domain:
         n = C.c_longlong()
         _check(lib().swe_gpu_launch_count(self.handle, C.byref(n)))
         return n.value
+
+    def lts_advance(self, t_end, max_iterations=1 << 20):
+        """local time stepping until the interval start time reaches t_end or
+        max_iterations inner iterations ran: (intervals finished, t)"""
+        n, t = C.c_int(), C.c_float()
+        rc = lib().swe_gpu_lts_advance(self.handle, float(t_end), int(max_iterations), C.byref(n), C.byref(t))
+        if rc != 1:  # SWE_GPU_INCOMPLETE: the iteration budget ran out first
+            _check(rc)
+        return n.value, t.value
+
+    def lts_state(self):
+        """(t, intervals, iterations, per-block steps of the last interval)"""
+        t, n, it = C.c_float(), C.c_int(), C.c_int()
+        steps = np.zeros(self.bx * self.by, dtype=np.int32)
+        _check(lib().swe_gpu_lts_state(self.handle, C.byref(t), C.byref(n), C.byref(it), _p(steps)))
+        return t.value, n.value, it.value, steps
+
+    def lts_blocks(self):
+        """per block: int[8] (layer states LEFT, RIGHT, BOTTOM, TOP, stepSize, stepSizeCounter,
+        timestepCounter, notified) and the layers' neighbour times float[4]"""
+        n = self.bx * self.by
+        ints = np.zeros((n, 8), dtype=np.int32)
+        border = np.zeros((n, 4), dtype=np.float32)
+        _check(lib().swe_gpu_lts_blocks(self.handle, _p(ints), _p(border)))
+        return ints, border
 
     def speed_pass_stats(self):
         """(bound tiles, tiles the last bounded speed pass evaluated edge by edge)"""
