@@ -225,6 +225,37 @@ def run_reference(args, world, rank):
     return 0
 
 
+def lts_measure(swe, device, intervals=6):
+    """Local time stepping at 2048^2 as 8x8 blocks of 256^2 over a 50 km
+    shoreline ramp (bathymetry -4000 m to +50 m across x, seeded Gaussian
+    bump), HLLE, synchronisation intervals of 1 s: blocks step at 2^k
+    substeps per interval.  One warm-up interval, then `intervals` timed ones
+    (host clock around the device-driven interval loop); cell-updates summed
+    over the blocks' own steps."""
+    n, nb = 2048, 64
+    geo, h, hu, hv, b = swe.init_domain(swe.SCENARIO_SHORELINE, n, n, nb, [SEED, 50000.0])
+    D = swe.Domain(geo["nx_cols"], geo["ny_rows"], geo["dx"], geo["dy"], boundary=geo["boundary"], solver=swe.HLLE,
+                   device=device, lts_max_timestep=1.0, duration=200.0)
+    D.upload(h, hu, hv, b)
+    D.exchange_bathymetry()
+    D.lts_advance(1.0)
+    cells = np.array([geo["nx_cols"][k // len(geo["ny_rows"])] * geo["ny_rows"][k % len(geo["ny_rows"])]
+                      for k in range(nb)], dtype=np.float64)
+    s0 = D.block_steps()
+    t0 = time.perf_counter()
+    done, t = D.lts_advance(1.0 + intervals)
+    el = time.perf_counter() - t0
+    s1 = D.block_steps()
+    _, _, iters, per_interval = D.lts_state()
+    updates = float(np.dot(cells, (s1 - s0).astype(np.float64)))
+    D.close()
+    levels = sorted(set(int(v) for v in per_interval))
+    return {"workload": "local time stepping, shoreline ramp 2048x2048 as 8x8 blocks of 256^2, HLLE, 1 s intervals",
+            "value": updates / el, "unit": "cell-updates/s (sum over blocks of cells x own steps)",
+            "intervals": done, "seconds": el, "block_steps_per_interval": levels,
+            "mean_steps_per_block_interval": float(np.mean((s1 - s0) / max(1, done)))}
+
+
 def run_gb300(args, world, rank, local):
     import torch
     import swe_gb300 as swe
@@ -326,6 +357,7 @@ def run_gb300(args, world, rank, local):
     except Exception:
         pass
 
+    lts = lts_measure(swe, local)
     base = cpu_baseline(float(os.environ.get("SWE_CPU_BASELINE_SECONDS", "12"))) if rank == 0 else None
     if rank == 0:
         line = {
@@ -343,6 +375,7 @@ def run_gb300(args, world, rank, local):
             "e2e": {"value": world * cells / e2e_s, "unit": "cell-updates/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "clocks": clk.summary(), "gpu_launches": launches, "device_status": status,
+            "lts": lts,
         }
         print(json.dumps(line), flush=True)
     D.close()

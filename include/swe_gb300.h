@@ -162,6 +162,9 @@ int swe_gpu_step(swe_gpu_domain *dom, int nsteps);
  * graph; returns the executed steps and the float time reached */
 int swe_gpu_advance(swe_gpu_domain *dom, float t_end, int max_steps, int *steps_done, float *t_now);
 int swe_gpu_get_time(swe_gpu_domain *dom, float *t, int *steps);
+/* Update steps every block has executed (one entry per block; under local
+ * time stepping blocks step at different rates).  Synchronises. */
+int swe_gpu_block_steps(swe_gpu_domain *dom, long long *steps);
 /* Local time stepping (domains created with lts_max_timestep > 0): runs
  * synchronisation intervals of every block at its own power-of-two share of
  * the interval, with time-interpolated ghost layers (src/blocks/SWE_Block.hh:311-562,

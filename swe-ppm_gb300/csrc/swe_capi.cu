@@ -993,6 +993,16 @@ int swe_gpu_lts_state(swe_gpu_domain *dom, float *t, int *intervals, int *iterat
     return SWE_GPU_OK;
 }
 
+int swe_gpu_block_steps(swe_gpu_domain *dom, long long *steps) {
+    if (!dom || !steps) return fail(SWE_GPU_ERR_INVALID, "null argument");
+    CUDA_TRY(cudaSetDevice(dom->device));
+    std::vector<GroupState> g;
+    int rc = readGroups(dom, g);
+    if (rc) return rc;
+    for (size_t k = 0; k < dom->blocks.size(); k++) steps[k] = g[dom->blocks[k].group].steps;
+    return SWE_GPU_OK;
+}
+
 int swe_gpu_lts_blocks(swe_gpu_domain *dom, int *ints, float *border) {
     if (!dom || !ints || !border) return fail(SWE_GPU_ERR_INVALID, "null argument");
     if (!dom->lts) return fail(SWE_GPU_ERR_INVALID, "not a local-time-stepping domain");

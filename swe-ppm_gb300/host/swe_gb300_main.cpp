@@ -6,7 +6,9 @@
 // rank), plus --blocks N (overdecomposition into a near-square block grid),
 // --solver hlle|fwave|augrie|hybrid, --semantics unsplit|split, --scenario and
 // --seed.  The time loop `while (t < checkpoint) step` of
-// src/examples/swe_mpi.cpp:300-327 runs on the device (swe_gpu_advance); at
+// src/examples/swe_mpi.cpp:300-327 runs on the device (swe_gpu_advance, or
+// swe_gpu_lts_advance with -l > 0: local time stepping with intervals of that
+// length, src/examples/swe_mpi_overdecomp.cpp:308-343); at
 // every checkpoint each block's state is snapshotted asynchronously into
 // pinned buffers and a writer thread appends it to the block's NetCDF file
 // while the next interval runs.  A Collector-style CSV line (PE_COUNT,
@@ -15,6 +17,7 @@
 // model is appended to <output>.log.
 #include <getopt.h>
 
+#include <algorithm>
 #include <chrono>
 #include <condition_variable>
 #include <cstdio>
@@ -66,6 +69,7 @@ struct Slot {
 int main(int argc, char **argv) {
     float duration = 0.f;
     int checkpoints = 1, nx = 0, ny = 0, nblocks = 1, write = 0, semantics = SWE_SEMANTICS_UNSPLIT;
+    float ltsInterval = 0.f;  // -l: local time stepping with intervals of this length
     std::string out = "swe", scenario = "radial_bathymetry_dam_break", solver = "hlle";
     double seed = 20261203;
     static option opts[] = {{"simulation-duration", required_argument, 0, 't'},
@@ -90,12 +94,7 @@ int main(int argc, char **argv) {
         case 'y': ny = atoi(optarg); break;
         case 'o': out = optarg; break;
         case 'w': write = atoi(optarg); break;
-        case 'l':
-            if (atof(optarg) > 0) {
-                fprintf(stderr, "swe_gb300: local time stepping is not available in this driver\n");
-                return 1;
-            }
-            break;
+        case 'l': ltsInterval = float(atof(optarg)); break;
         case 'b': nblocks = atoi(optarg); break;
         case 's': solver = optarg; break;
         case 'm': semantics = std::string(optarg) == "split" ? SWE_SEMANTICS_SPLIT : SWE_SEMANTICS_UNSPLIT; break;
@@ -148,6 +147,8 @@ int main(int argc, char **argv) {
     for (int i = 0; i < 4; i++) d.boundary[i] = outer[i];
     d.solver = solverId(solver);
     d.semantics = semantics;
+    d.lts_max_timestep = ltsInterval;
+    d.duration = duration;
     swe_gpu_domain *dom = nullptr;
     if (swe_gpu_domain_create(&d, &dom)) die("swe_gpu_domain_create");
 
@@ -221,8 +222,13 @@ int main(int argc, char **argv) {
     float t = 0.f;
     for (int i = 0; i < checkpoints; i++) {
         int n = 0;
-        if (swe_gpu_advance(dom, cp[i], 1 << 30, &n, &t)) die("advance");
-        steps += n;
+        if (ltsInterval > 0.f) {
+            // the drivers' `while (t < checkpoint)` over synchronisation intervals
+            if (swe_gpu_lts_advance(dom, cp[i], 1 << 30, &n, &t)) die("local time stepping");
+        } else {
+            if (swe_gpu_advance(dom, cp[i], 1 << 30, &n, &t)) die("advance");
+            steps += n;
+        }
         printf("Write timestep (%fs)\n", t);
         if (write) {
             Slot &s = slots[i & 1];
@@ -253,8 +259,17 @@ int main(int argc, char **argv) {
         for (auto &s : slots)
             for (void *p : s.bufs) swe_gpu_free_pinned(p);
     }
-    const double flops = 2.0 * double(nx) * double(ny) * 135.0 * double(steps);
-    const double cellUpdates = double(nx) * double(ny) * double(steps);
+    // cell updates summed over blocks (under local time stepping blocks step
+    // at their own rates)
+    std::vector<long long> blockSteps(size_t(bx) * by);
+    if (swe_gpu_block_steps(dom, blockSteps.data())) die("block steps");
+    double cellUpdates = 0.0;
+    steps = 0;
+    for (int k = 0; k < bx * by; k++) {
+        cellUpdates += double(cols[k / by]) * double(rows[k % by]) * double(blockSteps[k]);
+        steps = std::max(steps, blockSteps[k]);
+    }
+    const double flops = 2.0 * 135.0 * cellUpdates;
     printf("Flop count: %g\nFlops: %gGFLOPS\nWall Time: %gs\nSteps: %lld\nCell updates: %g/s\n", flops,
            1e-9 * flops / wall, wall, steps, cellUpdates / wall);
     const std::string logName = out + ".log";

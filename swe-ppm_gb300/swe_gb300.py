@@ -43,6 +43,7 @@ EXPORTED = [
     "swe_gpu_get_stream", "swe_gpu_set_stream", "swe_gpu_last_error", "swe_gpu_version", "swe_gpu_solve_edges", "swe_gpu_step_block_noalloc",
     "swe_gpu_snapshot_slabs_async", "swe_gpu_snapshot_wait", "swe_gpu_alloc_pinned", "swe_gpu_free_pinned",
     "swe_gpu_launch_count", "swe_gpu_speed_pass_stats", "swe_gpu_lts_advance", "swe_gpu_lts_state", "swe_gpu_lts_blocks",
+    "swe_gpu_block_steps",
     "swe_nc_open", "swe_nc_write_step", "swe_nc_write_step_slabs", "swe_nc_close",
     "swe_host_scenario_geometry", "swe_host_scenario_boundary", "swe_host_init_block", "swe_host_decompose",
 ]
@@ -101,6 +102,7 @@ def lib():
         L.swe_gpu_lts_advance.argtypes = [vp, C.c_float, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_float)]
         L.swe_gpu_lts_state.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_int), C.POINTER(C.c_int), vp]
         L.swe_gpu_lts_blocks.argtypes = [vp, vp, vp]
+        L.swe_gpu_block_steps.argtypes = [vp, vp]
         L.swe_gpu_set_time.argtypes = [vp, C.c_float]
         L.swe_gpu_status.argtypes = [vp, C.POINTER(C.c_int)]
         L.swe_gpu_get_stream.argtypes = [vp, C.POINTER(vp)]
@@ -331,6 +333,12 @@ class Domain:
         steps = np.zeros(self.bx * self.by, dtype=np.int32)
         _check(lib().swe_gpu_lts_state(self.handle, C.byref(t), C.byref(n), C.byref(it), _p(steps)))
         return t.value, n.value, it.value, steps
+
+    def block_steps(self):
+        """update steps each block has executed"""
+        out = np.zeros(self.bx * self.by, dtype=np.int64)
+        _check(lib().swe_gpu_block_steps(self.handle, _p(out)))
+        return out
 
     def lts_blocks(self):
         """per block: int[8] (layer states LEFT, RIGHT, BOTTOM, TOP, stepSize, stepSizeCounter,

@@ -67,3 +67,34 @@ def test_driver_checkpoints_match_oracle(swe, oracle_mod, tmp_path):
                 expect = a[offs[k]:offs[k + 1]].reshape(bnx + 2, bny + 2)[1:-1, 1:-1].T
                 assert_bitwise(f.variables[name][i + 1], expect, "block %d %s checkpoint %d" % (k, name, i))
         f.close()
+
+
+def test_driver_local_timestepping_matches_oracle(swe, oracle_mod, tmp_path):
+    """swe_gb300 -l 1: the checkpoint loop over synchronisation intervals,
+    NetCDF output bit-identical to the oracle's local time stepping."""
+    exe = os.path.join(os.path.dirname(swe.LIB_PATH), "swe_gb300")
+    base = str(tmp_path / "lts")
+    nx, ny, nb, T, ncp = 128, 96, 16, 3.0, 3
+    r = subprocess.run([exe, "-t", str(T), "-n", str(ncp), "-x", str(nx), "-y", str(ny), "-o", base, "-w", "1",
+                        "--blocks", str(nb), "--solver", "hlle", "-l", "1", "--scenario", "shoreline", "--seed", "11"],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    geo, h, hu, hv, b = swe.init_domain(swe.SCENARIO_SHORELINE, nx, ny, nb, [11, 50000.0])
+    R = oracle_mod.Domain(geo["nx_cols"], geo["ny_rows"], geo["dx"], geo["dy"], outer=geo["boundary"], solver=4,
+                          lts_max_timestep=1.0, duration=T)
+    R.set_state(h, hu, hv, b)
+    R.bathymetry_ghosts()
+    for _ in range(ncp):
+        assert R.lts_interval()[0] > 0
+    st = R.get_state()
+    by = len(geo["ny_rows"])
+    offs = np.cumsum([0] + [(geo["nx_cols"][k // by] + 2) * (geo["ny_rows"][k % by] + 2)
+                            for k in range(len(geo["nx_cols"]) * by)])
+    for k in range(len(geo["nx_cols"]) * by):
+        f = scipy_io.netcdf_file("%s_%d.nc" % (base, k), "r", mmap=False)
+        bnx, bny = geo["nx_cols"][k // by], geo["ny_rows"][k % by]
+        assert len(f.variables["time"][:]) == ncp + 1
+        for name, a in zip(("ah", "hu", "hv"), st[:3]):
+            expect = a[offs[k]:offs[k + 1]].reshape(bnx + 2, bny + 2)[1:-1, 1:-1].T
+            assert_bitwise(f.variables[name][ncp], expect, "block %d %s" % (k, name))
+        f.close()
