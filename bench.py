@@ -256,6 +256,38 @@ def lts_measure(swe, device, intervals=6):
             "mean_steps_per_block_interval": float(np.mean((s1 - s0) / max(1, done)))}
 
 
+def ensemble_measure(swe, device, steps=100, count=256):
+    """Batched ensemble: 256 independent radial dam breaks (nx, ny uniform in
+    64, 96, ..., 1024; radius U(0.05, 0.3) L; inner height U(5, 20) m, outer
+    U(1, 5) m; b = 0; one seed) in one handle, tile shape chosen by the tuner,
+    100 steps each at its own CFL dt, captured-graph replay (swe_gpu_advance).
+    Cell-updates summed over the instances."""
+    import torch
+    inst, states = swe.dam_break_ensemble(count, seed=SEED)
+    E = swe.Ensemble(inst, solver=swe.HLLE, device=device)
+    E.upload(*[np.concatenate([st[i] for st in states]) for i in range(4)])
+    E.exchange_bathymetry()
+    rows, cols, _ = E.autotune(trial_steps=3)
+    E.advance(1e30, max_steps=16)  # warm-up (graph capture)
+    stream = torch.cuda.Stream()
+    E.set_stream(stream.cuda_stream)
+    s0 = E.group_state()[2].astype(np.int64)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+        n, _ = E.advance(1e30, max_steps=steps)
+        e1.record(stream)
+        stream.synchronize()
+    ms = e0.elapsed_time(e1)
+    s1 = E.group_state()[2].astype(np.int64)
+    cells = np.array([nx * ny for nx, ny, *_ in inst], dtype=np.float64)
+    updates = float(np.dot(cells, (s1 - s0).astype(np.float64)))
+    E.close()
+    return {"workload": "256 radial dam breaks, nx, ny in 64..1024, HLLE, unsplit, own dt each, graph replay",
+            "value": updates / (ms * 1e-3), "unit": "cell-updates/s (sum over instances)", "steps": int(n),
+            "cells": int(cells.sum()), "ms": ms, "tile_rows": rows, "tile_cols": cols}
+
+
 def run_gb300(args, world, rank, local):
     import torch
     import swe_gb300 as swe
@@ -358,6 +390,7 @@ def run_gb300(args, world, rank, local):
         pass
 
     lts = lts_measure(swe, local)
+    ens = ensemble_measure(swe, local)
     base = cpu_baseline(float(os.environ.get("SWE_CPU_BASELINE_SECONDS", "12"))) if rank == 0 else None
     if rank == 0:
         line = {
@@ -375,7 +408,7 @@ def run_gb300(args, world, rank, local):
             "e2e": {"value": world * cells / e2e_s, "unit": "cell-updates/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "clocks": clk.summary(), "gpu_launches": launches, "device_status": status,
-            "lts": lts,
+            "lts": lts, "ensemble": ens,
         }
         print(json.dumps(line), flush=True)
     D.close()

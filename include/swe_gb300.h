@@ -102,6 +102,24 @@ typedef struct swe_gpu_desc {
 } swe_gpu_desc;
 
 int swe_gpu_domain_create(const swe_gpu_desc *desc, swe_gpu_domain **out);
+
+/* One independent simulation of an ensemble: a single block with its own
+ * size, cell size and boundary types. */
+typedef struct swe_gpu_instance {
+    int nx, ny;          /* interior cells */
+    float dx, dy;
+    int boundary[4];     /* LEFT, RIGHT, BOTTOM, TOP (no CONNECT_WITHIN_RANK) */
+} swe_gpu_instance;
+
+/* An ensemble: `count` independent instances in one domain handle, each its
+ * own dt group (own CFL time step, own clock), stepped together by the same
+ * persistent launches (swe_gpu_step, swe_gpu_advance; graph replay).  Block k
+ * is instance k for uploads, downloads and snapshots.  From `options` only
+ * solver, semantics, split_dt_mode, tile_rows, tile_cols, device,
+ * kernel_variant and speed_pass are used.  The reference runs independent
+ * scenarios as separate processes; this has no counterpart there. */
+int swe_gpu_ensemble_create(const swe_gpu_instance *instances, int count, const swe_gpu_desc *options,
+                            swe_gpu_domain **out);
 int swe_gpu_domain_destroy(swe_gpu_domain *dom);
 int swe_gpu_block_count(const swe_gpu_domain *dom, int *count);
 int swe_gpu_block_shape(const swe_gpu_domain *dom, int block, int *nx, int *ny);
@@ -183,6 +201,21 @@ int swe_gpu_lts_state(swe_gpu_domain *dom, float *t, int *intervals, int *iterat
  * sync, 4 next), stepSize, stepSizeCounter, timestepCounter, last-timestep
  * notice; border[4k..4k+3] = the neighbours' local times of the layers. */
 int swe_gpu_lts_blocks(swe_gpu_domain *dom, int *ints, float *border);
+/* dt groups (1 for a grid of blocks, one per instance of an ensemble or per
+ * block under local time stepping) and their clocks: time, last dt and steps
+ * (arrays of group-count entries, any may be null).  Synchronises. */
+int swe_gpu_group_count(const swe_gpu_domain *dom, int *count);
+int swe_gpu_group_state(swe_gpu_domain *dom, float *time, float *dt, int *steps);
+
+/* Re-partitions the step kernels' work for another tile shape (rows per CTA,
+ * a multiple of 32 up to 256; cap on columns per work segment, 0 = balanced
+ * default).  The state is untouched; results do not depend on the shape. */
+int swe_gpu_retile(swe_gpu_domain *dom, int tile_rows, int tile_cols);
+/* Tile-shape tuner: times `trial_steps` steps for each candidate shape on a
+ * copy of the current state (restored after every trial), keeps the fastest
+ * and reports it.  Needs room for one more copy of h, hu, hv. */
+int swe_gpu_autotune(swe_gpu_domain *dom, int trial_steps, int *best_rows, int *best_cols, float *best_ms);
+
 /* Kernels this domain has enqueued so far (a replay of the captured step
  * graph counts each of its kernel nodes); no synchronisation. */
 int swe_gpu_launch_count(const swe_gpu_domain *dom, long long *count);

@@ -117,6 +117,12 @@ __global__ void ghostKernel(const DomainDev d, int bathymetry) {
     }
 }
 
+/// the target time of every group (steps run while time < target)
+__global__ void setTargetsKernel(GroupState *g, int n, float target) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) g[i].target = target;
+}
+
 /// per-edge solver over arrays (solver::X<float>::computeNetUpdates)
 template <int S>
 __global__ void solveEdgesKernel(long long n, const float *hL, const float *hR, const float *huL, const float *huR,
@@ -216,6 +222,7 @@ struct swe_gpu_domain {
     int solver = SOLVER_HLLE, semantics = SEM_UNSPLIT, splitDtMode = SPLIT_DT_MAX;
     int variant = VARIANT_WARP;
     int tileRows = 256, tileCols = 32;
+    int tileColsArg = 0;              // segment-length cap asked for (0: default)
     std::vector<BlockDesc> blocks;
     std::vector<WorkUnit> units;
     std::vector<GroupState> groupsInit;
@@ -330,8 +337,8 @@ int readGroups(swe_gpu_domain *D, std::vector<GroupState> &g) {
 }
 
 int setTargets(swe_gpu_domain *D, float target) {
-    for (int g = 0; g < D->ngroups; g++)
-        CUDA_TRY(cudaMemcpyAsync(&D->dGroups[g].target, &target, sizeof(float), cudaMemcpyHostToDevice, D->stream));
+    setTargetsKernel<<<(D->ngroups + 255) / 256, 256, 0, D->stream>>>(D->dGroups, D->ngroups, target);
+    CUDA_TRY(cudaGetLastError());
     CUDA_TRY(cudaStreamSynchronize(D->stream));
     return SWE_GPU_OK;
 }
@@ -378,89 +385,35 @@ const char *swe_gpu_last_error(void) { return g_lastError.c_str(); }
 
 int swe_gpu_version(void) { return 1; }
 
-int swe_gpu_domain_create(const swe_gpu_desc *desc, swe_gpu_domain **out) {
-    if (!desc || !out) return fail(SWE_GPU_ERR_INVALID, "null descriptor or output pointer");
-    *out = nullptr;
-    const int bx = desc->blocks_x, by = desc->blocks_y;
-    if (bx < 1 || by < 1 || !desc->nx_cols || !desc->ny_rows)
-        return fail(SWE_GPU_ERR_INVALID, "need at least one block and the block sizes");
-    if (!(desc->dx > 0.f) || !(desc->dy > 0.f)) return fail(SWE_GPU_ERR_INVALID, "dx, dy must be positive");
-    if (desc->solver < SWE_SOLVER_FWAVE || desc->solver > SWE_SOLVER_HLLE)
-        return fail(SWE_GPU_ERR_INVALID, "unknown solver %d", desc->solver);
-    if (desc->semantics != SWE_SEMANTICS_UNSPLIT && desc->semantics != SWE_SEMANTICS_SPLIT)
-        return fail(SWE_GPU_ERR_INVALID, "unknown semantics %d", desc->semantics);
-    if (desc->semantics == SWE_SEMANTICS_SPLIT && bx * by != 1)
-        return fail(SWE_GPU_ERR_INVALID, "the split step is defined for a single block");
-    if (desc->lts_max_timestep > 0.f && desc->semantics != SWE_SEMANTICS_UNSPLIT)
-        return fail(SWE_GPU_ERR_INVALID, "local time stepping is defined for the unsplit step");
-    for (int i = 0; i < 4; i++)
-        if (desc->boundary[i] < SWE_OUTFLOW || desc->boundary[i] > SWE_PASSIVE)
-            return fail(SWE_GPU_ERR_INVALID, "unknown boundary type %d", desc->boundary[i]);
-    for (int i = 0; i < bx; i++)
-        if (desc->nx_cols[i] < 1) return fail(SWE_GPU_ERR_INVALID, "block width must be >= 1");
-    for (int i = 0; i < by; i++)
-        if (desc->ny_rows[i] < 1) return fail(SWE_GPU_ERR_INVALID, "block height must be >= 1");
-    int tileRows = desc->tile_rows > 0 ? desc->tile_rows : 256;
-    int tileCols = desc->tile_cols > 0 ? desc->tile_cols : 32;
-    if (tileRows % 32 != 0 || tileRows > kMaxTileRows) return fail(SWE_GPU_ERR_INVALID, "tile_rows must be a multiple of 32 <= %d", kMaxTileRows);
-    if (tileCols > kMaxTileCols) return fail(SWE_GPU_ERR_INVALID, "tile_cols must be <= %d", kMaxTileCols);
+namespace {
 
-    auto *D = new swe_gpu_domain();
-    D->device = desc->device;
-    D->lts = desc->lts_max_timestep > 0.f;
-    D->solver = desc->solver;
-    D->semantics = desc->semantics;
-    D->splitDtMode = desc->split_dt_mode;
-    D->variant = desc->kernel_variant == 1   ? VARIANT_WARP
-                 : desc->kernel_variant == 2 ? VARIANT_WARP2
-                 : desc->kernel_variant == 3 ? VARIANT_WARP1
-                                             : VARIANT_TILE;
-    int maxNy = 0;
-    for (int i = 0; i < by; i++) maxNy = std::max(maxNy, desc->ny_rows[i]);
-    D->tileRows = std::min(tileRows, ((maxNy + 31) / 32) * 32);
-    D->tileCols = tileCols;
+/// one block before layout: interior size, cell size, sides, dt group
+struct BlockSpec {
+    int nx, ny;
+    float dx, dy;
+    int bnd[4];  // boundary types; CONNECT_WITHIN_RANK where nbr >= 0
+    int nbr[4];
+    int group;
+};
 
-    cudaError_t e = cudaSetDevice(D->device);
-    if (e != cudaSuccess) {
-        delete D;
-        return fail(SWE_GPU_ERR_CUDA, "cudaSetDevice(%d): %s", desc->device, cudaGetErrorString(e));
-    }
-    e = cudaStreamCreateWithFlags(&D->ownStream, cudaStreamNonBlocking);
-    D->stream = D->ownStream;
-    if (e != cudaSuccess) {
-        delete D;
-        return fail(SWE_GPU_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
-    }
+struct DomainOptions {
+    int device, solver, semantics, splitDtMode, variant, tileRows, tileCols, speedPass;
+    float ltsMaxTimestep, duration;
+    int ngroups;
+};
 
-    // block descriptors and field layout
-    size_t elems = 0;
-    for (int k = 0; k < bx * by; k++) {
-        const int px = k / by, py = k % by;
-        BlockDesc B{};
-        B.nx = desc->nx_cols[px];
-        B.ny = desc->ny_rows[py];
-        B.pitch = ((B.ny + 2 + kColPad) + 31) / 32 * 32;
-        B.group = D->lts ? k : 0;  // local time stepping: every block its own dt group
-        B.base = (long long)elems + kColPad;
-        B.ring = D->ringElems;
-        D->ringElems += 2LL * (B.nx + B.ny);
-        B.dx = desc->dx;
-        B.dy = desc->dy;
-        const int nb[4] = {px > 0 ? k - by : -1, px < bx - 1 ? k + by : -1, py > 0 ? k - 1 : -1,
-                           py < by - 1 ? k + 1 : -1};
-        for (int s = 0; s < 4; s++) {
-            B.nbr[s] = nb[s];
-            B.bnd[s] = nb[s] >= 0 ? CONNECT_WITHIN_RANK : desc->boundary[s];
-        }
-        elems += size_t(B.nx + 2) * size_t(B.pitch);
-        B.stage = D->stageElems;
-        D->stageElems += (long long)(B.nx + 2) * (long long)(B.ny + 2);
-        D->maxCols = std::max(D->maxCols, B.nx + 2);
-        D->maxPerimeter = std::max(D->maxPerimeter, 2 * B.nx + 2 * B.ny + 4);
-        D->blocks.push_back(B);
-    }
-    elems += 32;  // slack so the last column's padding stays inside the allocation
-    D->fieldElems = elems;
+int variantOf(int kernelVariant) {
+    return kernelVariant == 1 ? VARIANT_WARP : kernelVariant == 2 ? VARIANT_WARP2 : kernelVariant == 3 ? VARIANT_WARP1
+                                                                                                       : VARIANT_TILE;
+}
+
+/// Balanced persistent partitions of both passes for the domain's current
+/// tile shape; tileColsArg > 0 caps the segment length.
+void buildPartitions(swe_gpu_domain *D, int tileColsArg) {
+    D->units.clear();
+    D->unitsU.clear();
+    D->ctaSeg.clear();
+    D->ctaSegU.clear();
     // Balanced persistent partitions, one per pass (the two kernels differ in
     // registers and therefore in resident CTAs): the (row tile, column) pairs
     // of all blocks in order, split into `workers` equal runs (a worker is a
@@ -478,7 +431,7 @@ int swe_gpu_domain_create(const swe_gpu_desc *desc, swe_gpu_domain **out) {
         long long total = 0;
         for (const BlockDesc &B : D->blocks) total += (long long)((B.ny + rowsPerTile - 1) / rowsPerTile) * B.nx;
         long long workers = (long long)sms * perSM;
-        if (desc->tile_cols > 0) workers = std::max(workers, (total + desc->tile_cols - 1) / desc->tile_cols);
+        if (tileColsArg > 0) workers = std::max(workers, (total + tileColsArg - 1) / tileColsArg);
         workers = std::max(1LL, std::min(total, workers));
         if (warp) workers = (workers + 3) / 4 * 4;  // whole CTAs of 4 warps
         std::vector<WorkUnit> &units = pass ? D->unitsU : D->units;
@@ -493,7 +446,7 @@ int swe_gpu_domain_create(const swe_gpu_desc *desc, swe_gpu_domain **out) {
             while (pos < end) {
                 const BlockDesc &B = D->blocks[k];
                 const long long take = std::min<long long>(end - pos, (long long)(B.nx + 1 - col));
-                const int cap = desc->tile_cols > 0 ? desc->tile_cols : (warp ? (1 << 30) : kMaxTileCols);
+                const int cap = tileColsArg > 0 ? tileColsArg : (warp ? (1 << 30) : kMaxTileCols);
                 const int len = int(std::min<long long>(take, cap));
                 units.push_back(WorkUnit{k, 1 + tile * rowsPerTile, col, col + len});
                 pos += len;
@@ -509,12 +462,80 @@ int swe_gpu_domain_create(const swe_gpu_desc *desc, swe_gpu_domain **out) {
             ctaSeg.push_back(int(units.size()));
         }
     }
+}
+
+/// per-group work counts of the passes
+void groupCounts(swe_gpu_domain *D, std::vector<GroupState> &g) {
+    for (GroupState &x : g) {
+        x.units = 0;
+        x.unitsUpd = 0;
+        x.tiles = 0;
+    }
+    for (const WorkUnit &u : D->units) g[D->blocks[u.block].group].units++;
+    for (const WorkUnit &u : D->unitsU) g[D->blocks[u.block].group].unitsUpd++;
+    for (const TileInfo &t : D->tiles) g[t.group].tiles++;
+}
+
+int buildDomain(const std::vector<BlockSpec> &spec, const DomainOptions &o, swe_gpu_domain **out) {
+    auto *D = new swe_gpu_domain();
+    D->device = o.device;
+    D->lts = o.ltsMaxTimestep > 0.f;
+    D->solver = o.solver;
+    D->semantics = o.semantics;
+    D->splitDtMode = o.splitDtMode;
+    D->variant = o.variant;
+    D->tileColsArg = o.tileCols;
+    int maxNy = 0;
+    for (const BlockSpec &b : spec) maxNy = std::max(maxNy, b.ny);
+    D->tileRows = std::min(o.tileRows > 0 ? o.tileRows : 256, ((maxNy + 31) / 32) * 32);
+    D->tileCols = o.tileCols > 0 ? o.tileCols : 32;
+    const int tileColsArg = o.tileCols;
+
+    cudaError_t e = cudaSetDevice(D->device);
+    if (e != cudaSuccess) {
+        delete D;
+        return fail(SWE_GPU_ERR_CUDA, "cudaSetDevice(%d): %s", o.device, cudaGetErrorString(e));
+    }
+    e = cudaStreamCreateWithFlags(&D->ownStream, cudaStreamNonBlocking);
+    D->stream = D->ownStream;
+    if (e != cudaSuccess) {
+        delete D;
+        return fail(SWE_GPU_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
+    }
+
+    // block descriptors and field layout
+    size_t elems = 0;
+    for (const BlockSpec &bs : spec) {
+        BlockDesc B{};
+        B.nx = bs.nx;
+        B.ny = bs.ny;
+        B.pitch = ((B.ny + 2 + kColPad) + 31) / 32 * 32;
+        B.group = bs.group;
+        B.base = (long long)elems + kColPad;
+        B.ring = D->ringElems;
+        D->ringElems += 2LL * (B.nx + B.ny);
+        B.dx = bs.dx;
+        B.dy = bs.dy;
+        for (int s = 0; s < 4; s++) {
+            B.nbr[s] = bs.nbr[s];
+            B.bnd[s] = bs.bnd[s];
+        }
+        elems += size_t(B.nx + 2) * size_t(B.pitch);
+        B.stage = D->stageElems;
+        D->stageElems += (long long)(B.nx + 2) * (long long)(B.ny + 2);
+        D->maxCols = std::max(D->maxCols, B.nx + 2);
+        D->maxPerimeter = std::max(D->maxPerimeter, 2 * B.nx + 2 * B.ny + 4);
+        D->blocks.push_back(B);
+    }
+    elems += 32;  // slack so the last column's padding stays inside the allocation
+    D->fieldElems = elems;
+    buildPartitions(D, tileColsArg);
     // Bounded speed pass: bound tiles of 32 x 32 cells per block, numbered
     // block by block, column of tiles by column of tiles
     bool smallBlocks = true;
     for (const BlockDesc &B : D->blocks) smallBlocks = smallBlocks && B.nx < 65535 && B.ny < 65535;
     D->bounded = D->variant == VARIANT_TILE && D->semantics == SEM_UNSPLIT &&
-                 (D->solver == SOLVER_FWAVE || D->solver == SOLVER_HLLE) && desc->speed_pass == 0 && smallBlocks;
+                 (D->solver == SOLVER_FWAVE || D->solver == SOLVER_HLLE) && o.speedPass == 0 && smallBlocks;
     if (D->bounded) {
         int base = 0;
         for (BlockDesc &B : D->blocks) {
@@ -562,17 +583,15 @@ int swe_gpu_domain_create(const swe_gpu_desc *desc, swe_gpu_domain **out) {
         const long long want = ((long long)D->tiles.size() + 7) / 8;
         D->gridB = int(std::max(1LL, std::min(want, (long long)sms * std::max(1, occupancyBound(D->solver)))));
     }
-    // dt groups: the whole domain, or (local time stepping) one per block
-    D->ngroups = D->lts ? int(D->blocks.size()) : 1;
+    // dt groups
+    D->ngroups = o.ngroups;
     {
         GroupState g0{};
         g0.target = INFINITY;
         g0.enabled = D->lts ? 0 : 1;
         D->groupsInit.assign(D->ngroups, g0);
-        for (int g = 0; g < D->ngroups; g++) D->groupsInit[g].firstBlock = D->lts ? g : 0;
-        for (const WorkUnit &u : D->units) D->groupsInit[D->blocks[u.block].group].units++;
-        for (const WorkUnit &u : D->unitsU) D->groupsInit[D->blocks[u.block].group].unitsUpd++;
-        for (const TileInfo &t : D->tiles) D->groupsInit[t.group].tiles++;
+        for (int k = int(D->blocks.size()) - 1; k >= 0; k--) D->groupsInit[D->blocks[k].group].firstBlock = k;
+        groupCounts(D, D->groupsInit);
     }
 
     bool ok = true;
@@ -624,8 +643,8 @@ int swe_gpu_domain_create(const swe_gpu_desc *desc, swe_gpu_domain **out) {
         ltsInit.assign(D->blocks.size(), l0);
         ctlInit.t = 0.f;
         ctlInit.target = 0.f;  // nothing runs before swe_gpu_lts_advance
-        ctlInit.maxTimestepLocal = desc->lts_max_timestep;
-        ctlInit.duration = desc->duration;
+        ctlInit.maxTimestepLocal = o.ltsMaxTimestep;
+        ctlInit.duration = o.duration;
         ctlInit.maxDivisor = 1024;  // src/blocks/SWE_Block.hh:221
         cudaMemcpyAsync(D->dLts, ltsInit.data(), sizeof(LtsBlock) * ltsInit.size(), cudaMemcpyHostToDevice, D->stream);
         cudaMemcpyAsync(D->dLtsCtl, &ctlInit, sizeof(LtsControl), cudaMemcpyHostToDevice, D->stream);
@@ -678,6 +697,119 @@ int swe_gpu_domain_create(const swe_gpu_desc *desc, swe_gpu_domain **out) {
     }
     *out = D;
     return SWE_GPU_OK;
+}
+
+int checkCommon(int solver, int semantics, const int boundary[4]) {
+    if (solver < SWE_SOLVER_FWAVE || solver > SWE_SOLVER_HLLE) return fail(SWE_GPU_ERR_INVALID, "unknown solver %d", solver);
+    if (semantics != SWE_SEMANTICS_UNSPLIT && semantics != SWE_SEMANTICS_SPLIT)
+        return fail(SWE_GPU_ERR_INVALID, "unknown semantics %d", semantics);
+    for (int i = 0; i < 4; i++)
+        if (boundary[i] < SWE_OUTFLOW || boundary[i] > SWE_PASSIVE)
+            return fail(SWE_GPU_ERR_INVALID, "unknown boundary type %d", boundary[i]);
+    return SWE_GPU_OK;
+}
+
+int checkTiles(int tileRows, int tileCols) {
+    const int tr = tileRows > 0 ? tileRows : 256;
+    if (tr % 32 != 0 || tr > kMaxTileRows) return fail(SWE_GPU_ERR_INVALID, "tile_rows must be a multiple of 32 <= %d", kMaxTileRows);
+    if (tileCols > kMaxTileCols) return fail(SWE_GPU_ERR_INVALID, "tile_cols must be <= %d", kMaxTileCols);
+    return SWE_GPU_OK;
+}
+
+} // namespace
+
+int swe_gpu_domain_create(const swe_gpu_desc *desc, swe_gpu_domain **out) {
+    if (!desc || !out) return fail(SWE_GPU_ERR_INVALID, "null descriptor or output pointer");
+    *out = nullptr;
+    const int bx = desc->blocks_x, by = desc->blocks_y;
+    if (bx < 1 || by < 1 || !desc->nx_cols || !desc->ny_rows)
+        return fail(SWE_GPU_ERR_INVALID, "need at least one block and the block sizes");
+    if (!(desc->dx > 0.f) || !(desc->dy > 0.f)) return fail(SWE_GPU_ERR_INVALID, "dx, dy must be positive");
+    int rc = checkCommon(desc->solver, desc->semantics, desc->boundary);
+    if (rc) return rc;
+    if (desc->semantics == SWE_SEMANTICS_SPLIT && bx * by != 1)
+        return fail(SWE_GPU_ERR_INVALID, "the split step is defined for a single block");
+    if (desc->lts_max_timestep > 0.f && desc->semantics != SWE_SEMANTICS_UNSPLIT)
+        return fail(SWE_GPU_ERR_INVALID, "local time stepping is defined for the unsplit step");
+    for (int i = 0; i < bx; i++)
+        if (desc->nx_cols[i] < 1) return fail(SWE_GPU_ERR_INVALID, "block width must be >= 1");
+    for (int i = 0; i < by; i++)
+        if (desc->ny_rows[i] < 1) return fail(SWE_GPU_ERR_INVALID, "block height must be >= 1");
+    rc = checkTiles(desc->tile_rows, desc->tile_cols);
+    if (rc) return rc;
+    const bool lts = desc->lts_max_timestep > 0.f;
+    std::vector<BlockSpec> spec;
+    for (int k = 0; k < bx * by; k++) {
+        const int px = k / by, py = k % by;
+        BlockSpec b{};
+        b.nx = desc->nx_cols[px];
+        b.ny = desc->ny_rows[py];
+        b.dx = desc->dx;
+        b.dy = desc->dy;
+        const int nb[4] = {px > 0 ? k - by : -1, px < bx - 1 ? k + by : -1, py > 0 ? k - 1 : -1,
+                           py < by - 1 ? k + 1 : -1};
+        for (int s = 0; s < 4; s++) {
+            b.nbr[s] = nb[s];
+            b.bnd[s] = nb[s] >= 0 ? CONNECT_WITHIN_RANK : desc->boundary[s];
+        }
+        b.group = lts ? k : 0;  // local time stepping: every block its own dt group
+        spec.push_back(b);
+    }
+    DomainOptions o{};
+    o.device = desc->device;
+    o.solver = desc->solver;
+    o.semantics = desc->semantics;
+    o.splitDtMode = desc->split_dt_mode;
+    o.variant = variantOf(desc->kernel_variant);
+    o.tileRows = desc->tile_rows;
+    o.tileCols = desc->tile_cols;
+    o.speedPass = desc->speed_pass;
+    o.ltsMaxTimestep = desc->lts_max_timestep;
+    o.duration = desc->duration;
+    o.ngroups = lts ? bx * by : 1;
+    return buildDomain(spec, o, out);
+}
+
+int swe_gpu_ensemble_create(const swe_gpu_instance *inst, int count, const swe_gpu_desc *options,
+                            swe_gpu_domain **out) {
+    if (!inst || count < 1 || !options || !out) return fail(SWE_GPU_ERR_INVALID, "need instances, options and output");
+    *out = nullptr;
+    if (options->lts_max_timestep > 0.f)
+        return fail(SWE_GPU_ERR_INVALID, "ensembles step globally per instance (no local time stepping)");
+    int rc = checkTiles(options->tile_rows, options->tile_cols);
+    if (rc) return rc;
+    std::vector<BlockSpec> spec;
+    for (int i = 0; i < count; i++) {
+        rc = checkCommon(options->solver, options->semantics, inst[i].boundary);
+        if (rc) return rc;
+        if (inst[i].nx < 1 || inst[i].ny < 1 || !(inst[i].dx > 0.f) || !(inst[i].dy > 0.f))
+            return fail(SWE_GPU_ERR_INVALID, "instance %d: sizes must be positive", i);
+        for (int s = 0; s < 4; s++)
+            if (inst[i].boundary[s] == SWE_CONNECT_WITHIN_RANK)
+                return fail(SWE_GPU_ERR_INVALID, "instance %d: an instance is one block without neighbours", i);
+        BlockSpec b{};
+        b.nx = inst[i].nx;
+        b.ny = inst[i].ny;
+        b.dx = inst[i].dx;
+        b.dy = inst[i].dy;
+        for (int s = 0; s < 4; s++) {
+            b.bnd[s] = inst[i].boundary[s];
+            b.nbr[s] = -1;
+        }
+        b.group = i;
+        spec.push_back(b);
+    }
+    DomainOptions o{};
+    o.device = options->device;
+    o.solver = options->solver;
+    o.semantics = options->semantics;
+    o.splitDtMode = options->split_dt_mode;
+    o.variant = variantOf(options->kernel_variant);
+    o.tileRows = options->tile_rows;
+    o.tileCols = options->tile_cols;
+    o.speedPass = options->speed_pass;
+    o.ngroups = count;
+    return buildDomain(spec, o, out);
 }
 
 int swe_gpu_domain_destroy(swe_gpu_domain *dom) {
@@ -898,9 +1030,20 @@ int swe_gpu_advance(swe_gpu_domain *dom, float t_end, int max_steps, int *steps_
     std::vector<GroupState> g;
     int rc = readGroups(dom, g);
     if (rc) return rc;
-    const int startSteps = g[0].steps;
+    std::vector<int> startSteps(g.size());
+    for (size_t i = 0; i < g.size(); i++) startSteps[i] = g[i].steps;
     rc = setTargets(dom, t_end);
     if (rc) return rc;
+    // steps taken (the most any group took) and whether every group reached t_end
+    auto progress = [&](int &steps) {
+        steps = 0;
+        bool all = true;
+        for (size_t i = 0; i < g.size(); i++) {
+            steps = std::max(steps, g[i].steps - startSteps[i]);
+            all = all && !(g[i].time < t_end);
+        }
+        return all;
+    };
     int done = 0;
     while (done < max_steps) {
         const int remaining = max_steps - done;
@@ -915,14 +1058,19 @@ int swe_gpu_advance(swe_gpu_domain *dom, float t_end, int max_steps, int *steps_
         }
         rc = readGroups(dom, g);
         if (rc) return rc;
-        done = g[0].steps - startSteps;
-        if (!(g[0].time < t_end)) break;
+        if (progress(done)) break;
     }
     rc = setTargets(dom, INFINITY);
     if (rc) return rc;
     if (steps_done) *steps_done = done;
-    if (t_now) *t_now = g[0].time;
-    if (g[0].status) return fail(SWE_GPU_ERR_DEVICE, "device status 0x%x (NaN wave speed)", g[0].status);
+    float tmin = g[0].time;
+    int status = 0;
+    for (const GroupState &x : g) {
+        tmin = std::min(tmin, x.time);
+        status |= x.status;
+    }
+    if (t_now) *t_now = tmin;
+    if (status) return fail(SWE_GPU_ERR_DEVICE, "device status 0x%x (NaN wave speed)", status);
     return SWE_GPU_OK;
 }
 
@@ -1020,6 +1168,183 @@ int swe_gpu_lts_blocks(swe_gpu_domain *dom, int *ints, float *border) {
         ints[8 * k + 6] = L[k].timestepCounter;
         ints[8 * k + 7] = L[k].notified;
     }
+    return SWE_GPU_OK;
+}
+
+int swe_gpu_group_count(const swe_gpu_domain *dom, int *count) {
+    if (!dom || !count) return fail(SWE_GPU_ERR_INVALID, "null argument");
+    *count = dom->ngroups;
+    return SWE_GPU_OK;
+}
+
+int swe_gpu_group_state(swe_gpu_domain *dom, float *time, float *dt, int *steps) {
+    if (!dom) return fail(SWE_GPU_ERR_INVALID, "null domain handle");
+    CUDA_TRY(cudaSetDevice(dom->device));
+    std::vector<GroupState> g;
+    int rc = readGroups(dom, g);
+    if (rc) return rc;
+    for (size_t i = 0; i < g.size(); i++) {
+        if (time) time[i] = g[i].time;
+        if (dt) dt[i] = g[i].dt;
+        if (steps) steps[i] = g[i].steps;
+    }
+    return SWE_GPU_OK;
+}
+
+int swe_gpu_retile(swe_gpu_domain *dom, int tile_rows, int tile_cols) {
+    if (!dom) return fail(SWE_GPU_ERR_INVALID, "null domain handle");
+    int rc = checkTiles(tile_rows, tile_cols);
+    if (rc) return rc;
+    CUDA_TRY(cudaSetDevice(dom->device));
+    CUDA_TRY(cudaStreamSynchronize(dom->stream));
+    int maxNy = 0;
+    for (const BlockDesc &B : dom->blocks) maxNy = std::max(maxNy, B.ny);
+    dom->tileRows = std::min(tile_rows > 0 ? tile_rows : 256, ((maxNy + 31) / 32) * 32);
+    dom->tileColsArg = tile_cols;
+    dom->tileCols = tile_cols > 0 ? tile_cols : 32;
+    buildPartitions(dom, tile_cols);
+    // device copies of the new partitions; per-group segment counts
+    cudaFree(dom->dUnits);
+    cudaFree(dom->dCtaSeg);
+    cudaFree(dom->dUnitsU);
+    cudaFree(dom->dCtaSegU);
+    dom->dUnits = nullptr;
+    dom->dCtaSeg = nullptr;
+    dom->dUnitsU = nullptr;
+    dom->dCtaSegU = nullptr;
+    CUDA_TRY(cudaMalloc(&dom->dUnits, sizeof(WorkUnit) * dom->units.size()));
+    CUDA_TRY(cudaMalloc(&dom->dCtaSeg, sizeof(int) * dom->ctaSeg.size()));
+    CUDA_TRY(cudaMalloc(&dom->dUnitsU, sizeof(WorkUnit) * dom->unitsU.size()));
+    CUDA_TRY(cudaMalloc(&dom->dCtaSegU, sizeof(int) * dom->ctaSegU.size()));
+    CUDA_TRY(cudaMemcpy(dom->dUnits, dom->units.data(), sizeof(WorkUnit) * dom->units.size(), cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(dom->dCtaSeg, dom->ctaSeg.data(), sizeof(int) * dom->ctaSeg.size(), cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(dom->dUnitsU, dom->unitsU.data(), sizeof(WorkUnit) * dom->unitsU.size(), cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(dom->dCtaSegU, dom->ctaSegU.data(), sizeof(int) * dom->ctaSegU.size(), cudaMemcpyHostToDevice));
+    std::vector<GroupState> g;
+    rc = readGroups(dom, g);
+    if (rc) return rc;
+    groupCounts(dom, g);
+    CUDA_TRY(cudaMemcpy(dom->dGroups, g.data(), sizeof(GroupState) * g.size(), cudaMemcpyHostToDevice));
+    dom->dev.units = dom->dUnits;
+    dom->dev.ctaSeg = dom->dCtaSeg;
+    dom->dev.tileRows = dom->tileRows;
+    // captured step graphs hold the old launch shapes
+    if (dom->graph) cudaGraphExecDestroy(dom->graph);
+    if (dom->ltsGraph) cudaGraphExecDestroy(dom->ltsGraph);
+    dom->graph = nullptr;
+    dom->ltsGraph = nullptr;
+    return SWE_GPU_OK;
+}
+
+int swe_gpu_autotune(swe_gpu_domain *dom, int trial_steps, int *best_rows, int *best_cols, float *best_ms) {
+    if (!dom || trial_steps < 1) return fail(SWE_GPU_ERR_INVALID, "bad argument");
+    if (dom->lts) return fail(SWE_GPU_ERR_INVALID, "the tuner times global steps; not for local time stepping");
+    CUDA_TRY(cudaSetDevice(dom->device));
+    CUDA_TRY(cudaStreamSynchronize(dom->stream));
+    // save the state the trials run on, restore it after each
+    const size_t bytes = dom->fieldElems * sizeof(float);
+    std::vector<float *> save(6, nullptr);
+    float *live[6] = {dom->h[0], dom->h[1], dom->hu[0], dom->hu[1], dom->hv[0], dom->hv[1]};
+    GroupState *gsave = nullptr;
+    unsigned int *wsave = nullptr;
+    unsigned long long *ksave = nullptr;
+    const size_t nt = dom->tiles.size();
+    auto release = [&]() {
+        for (float *p : save) cudaFree(p);
+        cudaFree(gsave);
+        cudaFree(wsave);
+        cudaFree(ksave);
+    };
+    bool ok = true;
+    for (int i = 0; i < 6 && ok; i++) ok = cudaMalloc(&save[i], bytes) == cudaSuccess;
+    ok = ok && cudaMalloc(&gsave, sizeof(GroupState) * dom->ngroups) == cudaSuccess;
+    if (nt) {
+        ok = ok && cudaMalloc(&wsave, sizeof(unsigned int) * 2 * nt) == cudaSuccess;
+        ok = ok && cudaMalloc(&ksave, sizeof(unsigned long long) * 2 * nt) == cudaSuccess;
+    }
+    if (!ok) {
+        cudaGetLastError();
+        release();
+        return fail(SWE_GPU_ERR_NOMEM, "tuner: no room for a copy of the state");
+    }
+    const bool ghostsValid = dom->ghostsValid;
+    auto copyState = [&](bool toSave) -> cudaError_t {
+        for (int i = 0; i < 6; i++) {
+            cudaError_t e = cudaMemcpyAsync(toSave ? save[i] : live[i], toSave ? live[i] : save[i], bytes,
+                                            cudaMemcpyDeviceToDevice, dom->stream);
+            if (e != cudaSuccess) return e;
+        }
+        cudaError_t e = cudaMemcpyAsync(toSave ? gsave : dom->dGroups, toSave ? dom->dGroups : gsave,
+                                        sizeof(GroupState) * dom->ngroups, cudaMemcpyDeviceToDevice, dom->stream);
+        if (e == cudaSuccess && nt) {
+            e = cudaMemcpyAsync(toSave ? wsave : dom->dTileW, toSave ? dom->dTileW : wsave, sizeof(unsigned int) * 2 * nt,
+                                cudaMemcpyDeviceToDevice, dom->stream);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(toSave ? ksave : dom->dTileKey, toSave ? dom->dTileKey : ksave,
+                                    sizeof(unsigned long long) * 2 * nt, cudaMemcpyDeviceToDevice, dom->stream);
+        }
+        if (e == cudaSuccess) e = cudaStreamSynchronize(dom->stream);
+        dom->ghostsValid = ghostsValid;
+        if (e == cudaSuccess && !toSave) {
+            // the saved group states carry the saved partition's segment counts
+            std::vector<GroupState> g(dom->ngroups);
+            e = cudaMemcpy(g.data(), dom->dGroups, sizeof(GroupState) * g.size(), cudaMemcpyDeviceToHost);
+            groupCounts(dom, g);
+            if (e == cudaSuccess)
+                e = cudaMemcpy(dom->dGroups, g.data(), sizeof(GroupState) * g.size(), cudaMemcpyHostToDevice);
+        }
+        return e;
+    };
+    cudaError_t e = copyState(true);
+    if (e != cudaSuccess) {
+        release();
+        return fail(SWE_GPU_ERR_CUDA, "tuner: %s", cudaGetErrorString(e));
+    }
+    int maxNy = 0;
+    for (const BlockDesc &B : dom->blocks) maxNy = std::max(maxNy, B.ny);
+    const int rowCands[4] = {32, 64, 128, 256}, colCands[4] = {0, 8, 32, 128};
+    const int origRows = dom->tileRows, origCols = dom->tileColsArg;
+    int bestR = origRows, bestC = origCols;
+    float bestT = INFINITY;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    int rc = SWE_GPU_OK;
+    for (int r : rowCands) {
+        if (r > ((maxNy + 31) / 32) * 32 && r != 32) continue;
+        for (int c : colCands) {
+            if ((rc = swe_gpu_retile(dom, r, c))) break;
+            if ((e = copyState(false)) != cudaSuccess) break;
+            for (int i = 0; i < 2 && !rc; i++) rc = enqueueStep(dom);  // warm-up
+            cudaEventRecord(e0, dom->stream);
+            for (int i = 0; i < trial_steps && !rc; i++) rc = enqueueStep(dom);
+            cudaEventRecord(e1, dom->stream);
+            if (rc || (e = cudaEventSynchronize(e1)) != cudaSuccess) break;
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            ms /= float(trial_steps);
+            if (ms < bestT) {
+                bestT = ms;
+                bestR = dom->tileRows;
+                bestC = c;
+            }
+        }
+        if (rc || e != cudaSuccess) break;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    // the best shape, on the original state
+    const bool failed = rc || e != cudaSuccess;
+    const int rc2 = swe_gpu_retile(dom, failed ? origRows : bestR, failed ? origCols : bestC);
+    const cudaError_t e2 = copyState(false);
+    release();
+    if (rc) return rc;
+    if (e != cudaSuccess) return fail(SWE_GPU_ERR_CUDA, "tuner: %s", cudaGetErrorString(e));
+    if (rc2) return rc2;
+    if (e2 != cudaSuccess) return fail(SWE_GPU_ERR_CUDA, "tuner: %s", cudaGetErrorString(e2));
+    if (best_rows) *best_rows = bestR;
+    if (best_cols) *best_cols = bestC;
+    if (best_ms) *best_ms = bestT;
     return SWE_GPU_OK;
 }
 

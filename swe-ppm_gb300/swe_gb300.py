@@ -43,7 +43,8 @@ EXPORTED = [
     "swe_gpu_get_stream", "swe_gpu_set_stream", "swe_gpu_last_error", "swe_gpu_version", "swe_gpu_solve_edges", "swe_gpu_step_block_noalloc",
     "swe_gpu_snapshot_slabs_async", "swe_gpu_snapshot_wait", "swe_gpu_alloc_pinned", "swe_gpu_free_pinned",
     "swe_gpu_launch_count", "swe_gpu_speed_pass_stats", "swe_gpu_lts_advance", "swe_gpu_lts_state", "swe_gpu_lts_blocks",
-    "swe_gpu_block_steps",
+    "swe_gpu_block_steps", "swe_gpu_ensemble_create", "swe_gpu_group_count", "swe_gpu_group_state",
+    "swe_gpu_retile", "swe_gpu_autotune",
     "swe_nc_open", "swe_nc_write_step", "swe_nc_write_step_slabs", "swe_nc_close",
     "swe_host_scenario_geometry", "swe_host_scenario_boundary", "swe_host_init_block", "swe_host_decompose",
 ]
@@ -60,6 +61,11 @@ class Desc(C.Structure):
                 ("split_dt_mode", C.c_int), ("tile_rows", C.c_int), ("tile_cols", C.c_int), ("device", C.c_int),
                 ("kernel_variant", C.c_int), ("speed_pass", C.c_int), ("lts_max_timestep", C.c_float),
                 ("duration", C.c_float)]
+
+
+class Instance(C.Structure):
+    """one simulation of an ensemble (swe_gpu_instance)"""
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("dx", C.c_float), ("dy", C.c_float), ("boundary", C.c_int * 4)]
 
 
 _lib = None
@@ -103,6 +109,11 @@ def lib():
         L.swe_gpu_lts_state.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_int), C.POINTER(C.c_int), vp]
         L.swe_gpu_lts_blocks.argtypes = [vp, vp, vp]
         L.swe_gpu_block_steps.argtypes = [vp, vp]
+        L.swe_gpu_ensemble_create.argtypes = [C.POINTER(Instance), C.c_int, C.POINTER(Desc), C.POINTER(vp)]
+        L.swe_gpu_group_count.argtypes = [vp, C.POINTER(C.c_int)]
+        L.swe_gpu_group_state.argtypes = [vp, vp, vp, vp]
+        L.swe_gpu_retile.argtypes = [vp, C.c_int, C.c_int]
+        L.swe_gpu_autotune.argtypes = [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_float)]
         L.swe_gpu_set_time.argtypes = [vp, C.c_float]
         L.swe_gpu_status.argtypes = [vp, C.POINTER(C.c_int)]
         L.swe_gpu_get_stream.argtypes = [vp, C.POINTER(vp)]
@@ -334,6 +345,26 @@ class Domain:
         _check(lib().swe_gpu_lts_state(self.handle, C.byref(t), C.byref(n), C.byref(it), _p(steps)))
         return t.value, n.value, it.value, steps
 
+    def group_state(self):
+        """per dt group: (time, last dt, steps)"""
+        n = C.c_int()
+        _check(lib().swe_gpu_group_count(self.handle, C.byref(n)))
+        t = np.zeros(n.value, dtype=np.float32)
+        dt = np.zeros(n.value, dtype=np.float32)
+        st = np.zeros(n.value, dtype=np.int32)
+        _check(lib().swe_gpu_group_state(self.handle, _p(t), _p(dt), _p(st)))
+        return t, dt, st
+
+    def retile(self, tile_rows=0, tile_cols=0):
+        _check(lib().swe_gpu_retile(self.handle, int(tile_rows), int(tile_cols)))
+
+    def autotune(self, trial_steps=5):
+        """times the candidate tile shapes on a copy of the state, keeps the
+        fastest: (tile_rows, tile_cols, ms per step)"""
+        r, c, ms = C.c_int(), C.c_int(), C.c_float()
+        _check(lib().swe_gpu_autotune(self.handle, int(trial_steps), C.byref(r), C.byref(c), C.byref(ms)))
+        return r.value, c.value, ms.value
+
     def block_steps(self):
         """update steps each block has executed"""
         out = np.zeros(self.bx * self.by, dtype=np.int64)
@@ -381,6 +412,52 @@ class Domain:
     def set_stream(self, stream):
         """launch on an external cudaStream_t (int handle); None = own stream"""
         _check(lib().swe_gpu_set_stream(self.handle, C.c_void_p(stream or 0)))
+
+
+class Ensemble(Domain):
+    """Independent simulations (one block each, own size, cell size,
+    boundaries and dt) stepped together in one handle.  Block k = instance k."""
+
+    def __init__(self, instances, solver=HLLE, semantics=UNSPLIT, split_dt_mode=SPLIT_DT_MAX, tile_rows=0,
+                 tile_cols=0, device=0, kernel_variant=0, speed_pass=0):
+        n = len(instances)
+        arr = (Instance * n)()
+        for i, (nx, ny, dx, dy, bnd) in enumerate(instances):
+            arr[i].nx, arr[i].ny, arr[i].dx, arr[i].dy = int(nx), int(ny), float(dx), float(dy)
+            for s4 in range(4):
+                arr[i].boundary[s4] = int(bnd[s4])
+        d = Desc()
+        d.solver, d.semantics, d.split_dt_mode = int(solver), int(semantics), int(split_dt_mode)
+        d.tile_rows, d.tile_cols, d.device = int(tile_rows), int(tile_cols), int(device)
+        d.kernel_variant, d.speed_pass = int(kernel_variant), int(speed_pass)
+        self.handle = C.c_void_p()
+        _check(lib().swe_gpu_ensemble_create(arr, n, C.byref(d), C.byref(self.handle)))
+        self.bx, self.by = n, 1
+        self.nx_cols = [int(i[0]) for i in instances]
+        self.ny_rows = [int(i[1]) for i in instances]
+        self.shapes = [(int(i[0]), int(i[1])) for i in instances]
+        self.offsets = np.cumsum([0] + [(nx + 2) * (ny + 2) for nx, ny in self.shapes])
+        self.ncells = int(self.offsets[-1])
+
+
+def dam_break_ensemble(count, seed, sizes=None, length=1000.0):
+    """`count` radial dam breaks on a length x length square, b = 0, outflow
+    sides: nx, ny drawn from `sizes` (default 64, 96, ..., 1024), radius
+    U(0.05, 0.3) length, inner height U(5, 20) m, outer height U(1, 5) m, all
+    from one seed.  Returns (instances for Ensemble, [(h, hu, hv, b)] per instance)."""
+    rng = np.random.default_rng(seed)
+    sizes = np.arange(64, 1025, 32) if sizes is None else np.asarray(sizes)
+    inst, states = [], []
+    for _ in range(count):
+        nx, ny = int(rng.choice(sizes)), int(rng.choice(sizes))
+        radius = float(rng.uniform(0.05, 0.3)) * length
+        hin, hout = float(rng.uniform(5.0, 20.0)), float(rng.uniform(1.0, 5.0))
+        dx, dy = float(np.float32(length / nx)), float(np.float32(length / ny))
+        bnd = [OUTFLOW] * 4
+        states.append(init_block(SCENARIO_DAM_BREAK, nx, ny, dx, dy, 0.0, 0.0, bnd,
+                                 [length, radius, hin, hout, 0.0, 0.0, 0.0]))
+        inst.append((nx, ny, dx, dy, bnd))
+    return inst, states
 
 
 def solve_edges_device(solver, ptrs_in, ptrs_out, n, stream=None):
