@@ -17,7 +17,7 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libswe_gb300.so")
 DRIVER = os.path.join(OUT, "swe_gb300")
 
-CUDA_SOURCES = ["csrc/swe_capi.cu", "csrc/swe_kernels_fh.cu", "csrc/swe_kernels_aug.cu", "csrc/swe_lts.cu"]
+CUDA_SOURCES = ["csrc/swe_capi.cu", "csrc/swe_kernels_fh.cu", "csrc/swe_kernels_aug.cu", "csrc/swe_lts.cu", "csrc/swe_mlp.cu"]
 HOST_SOURCES = ["host/swe_host.cpp", "host/netcdf_writer.cpp"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-fmad=false", "-lineinfo", "-std=c++17",
               "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-I" + os.path.join(ROOT, "include")]
@@ -44,7 +44,7 @@ def _deps():
     for sub in ("csrc", "host"):
         d = os.path.join(HERE, sub)
         out += [os.path.join(d, f) for f in os.listdir(d)]
-    out.append(os.path.join(ROOT, "include", "swe_gb300.h"))
+    out += [os.path.join(ROOT, "include", f) for f in os.listdir(os.path.join(ROOT, "include"))]
     return out
 
 

@@ -45,6 +45,7 @@ EXPORTED = [
     "swe_gpu_launch_count", "swe_gpu_speed_pass_stats", "swe_gpu_lts_advance", "swe_gpu_lts_state", "swe_gpu_lts_blocks",
     "swe_gpu_block_steps", "swe_gpu_ensemble_create", "swe_gpu_group_count", "swe_gpu_group_state",
     "swe_gpu_retile", "swe_gpu_autotune",
+    "swe_mlp_last_error", "swe_mlp_gemm_check",
     "swe_nc_open", "swe_nc_write_step", "swe_nc_write_step_slabs", "swe_nc_close",
     "swe_host_scenario_geometry", "swe_host_scenario_boundary", "swe_host_init_block", "swe_host_decompose",
 ]
@@ -109,6 +110,8 @@ def lib():
         L.swe_gpu_lts_state.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_int), C.POINTER(C.c_int), vp]
         L.swe_gpu_lts_blocks.argtypes = [vp, vp, vp]
         L.swe_gpu_block_steps.argtypes = [vp, vp]
+        L.swe_mlp_last_error.restype = C.c_char_p
+        L.swe_mlp_gemm_check.argtypes = [C.c_int, C.c_int, vp, vp, vp]
         L.swe_gpu_ensemble_create.argtypes = [C.POINTER(Instance), C.c_int, C.POINTER(Desc), C.POINTER(vp)]
         L.swe_gpu_group_count.argtypes = [vp, C.POINTER(C.c_int)]
         L.swe_gpu_group_state.argtypes = [vp, vp, vp, vp]
@@ -438,6 +441,20 @@ class Ensemble(Domain):
         self.shapes = [(int(i[0]), int(i[1])) for i in instances]
         self.offsets = np.cumsum([0] + [(nx + 2) * (ny + 2) for nx, ny in self.shapes])
         self.ncells = int(self.offsets[-1])
+
+
+def _mlp_check(rc):
+    if rc != 0:
+        raise SweGpuError("swe_mlp error %d: %s" % (rc, lib().swe_mlp_last_error().decode()))
+
+
+def tc_gemm_check(a, b):
+    """D = A B^T on the tensor cores (BF16 in, FP32 out), A 128 x k, B n x k"""
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    b = np.ascontiguousarray(b, dtype=np.float32)
+    d = np.zeros((128, b.shape[0]), dtype=np.float32)
+    _mlp_check(lib().swe_mlp_gemm_check(b.shape[0], a.shape[1], _p(a), _p(b), _p(d)))
+    return d
 
 
 def dam_break_ensemble(count, seed, sizes=None, length=1000.0):
