@@ -16,10 +16,57 @@ extern "C" {
 
 const char *swe_mlp_last_error(void);
 
-/* Tensor-core self-check: D[128 x n] = A[128 x k] * B[n x k]^T with A and B
- * rounded to BF16 and FP32 accumulation, one CTA, host arrays (row-major).
- * n: 16..128, k: 16..64, multiples of 16. */
-int swe_mlp_gemm_check(int n, int k, const float *a, const float *b, float *d);
+/* Parameters: W1[64][6], b1[64], W2[64][64], b2[64], W3[64][64], b3[64],
+ * W4[4][64], b4[4] (row-major, rows = output neurons), FP32. */
+#define SWE_MLP_NPARAMS 9028
+int swe_mlp_param_count(void);
+
+/* Edge arrays are structure-of-arrays host memory of n edges each:
+ *   edges   = hL[n] hR[n] huL[n] huR[n] bL[n] bR[n]  (the argument order of
+ *             solver::X<float>::computeNetUpdates at the reference's call
+ *             sites, normal momentum)
+ *   targets = hUpdL[n] hUpdR[n] huUpdL[n] huUpdR[n]  (net updates to learn)
+ *   outputs = o0[n] o1[n] o2[n] o3[n]  (raw network outputs: speed
+ *             corrections of the two waves in units of sqrt(g h), predicted
+ *             strengths in units of h sqrt(g h)) */
+typedef struct swe_mlp swe_mlp;
+
+/* New surrogate on the current device: Glorot-uniform hidden weights from
+ * `seed`, zero biases and a zero last layer (the untrained surrogate is the
+ * f-wave solver with Roe speeds).  Allocates its device state. */
+int swe_mlp_create(unsigned long long seed, swe_mlp **out);
+void swe_mlp_destroy(swe_mlp *m);
+int swe_mlp_get_params(swe_mlp *m, float *params);
+/* Sets the FP32 master parameters and clears the optimiser state. */
+int swe_mlp_set_params(swe_mlp *m, const float *params);
+
+/* Raw network outputs (BF16 operands, FP32 accumulation) of n edges. */
+int swe_mlp_forward(swe_mlp *m, int n, const float *edges, float *outputs);
+
+/* Surrogate solve of n edges: net updates (4 x n, same order as targets),
+ * maximum wave speed, and used[e] = 1 where the surrogate's gate accepted
+ * the edge, 0 where the augmented Riemann solver computed it instead (a side
+ * shallower than 0.1 m, waves closer than 0.5 sqrt(g h), or predicted
+ * strengths inconsistent with the closure). */
+int swe_mlp_solve(swe_mlp *m, int n, const float *edges, float *updates, float *speed, unsigned char *used);
+
+/* Mean training loss over n edges and its gradient (SWE_MLP_NPARAMS floats). */
+int swe_mlp_loss_grad(swe_mlp *m, int n, const float *edges, const float *targets, float *loss, float *grad);
+
+/* Adam training (beta 0.9 / 0.999, eps 1e-8) for `epochs` passes over the n
+ * edges in shuffled mini-batches of `batch`; epoch_loss (may be NULL) gets the
+ * mean loss of each epoch, measured during the pass. */
+int swe_mlp_train(swe_mlp *m, int n, const float *edges, const float *targets, int epochs, int batch, float lr,
+                  unsigned long long seed, float *epoch_loss);
+
+/* Tensor-core self-check, one CTA, host arrays (row-major), operands rounded
+ * to BF16, FP32 accumulation:
+ *   mode 0: D[128 x w2] = X[128 x w1] Y[w2 x w1]^T   (both operands K-major)
+ *   mode 1: D[w1 x w2]  = X[128 x w1]^T Y[128 x w2]  (both read transposed, K = 128)
+ *   mode 2: D[128 x w2] = X[128 x w1] Y[w1 x w2]     (Y read transposed)
+ * D is returned as 128 x w2 (mode 1: rows >= w1 undefined).
+ * w1 in {16, 32, 64}; w2 16..128, a multiple of 16. */
+int swe_mlp_gemm_check(int mode, int w1, int w2, const float *x, const float *y, float *d);
 
 #ifdef __cplusplus
 }

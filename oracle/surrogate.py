@@ -139,7 +139,9 @@ def gate(aux, W):
 def loss_and_grad(p, edges, targets, rounding=True):
     """mean loss over the edges and its gradient (flat), as the GPU computes
     it: net-update error scaled by h c (h updates) and h c^2 (hu updates), plus
-    LAMBDA times the strength inconsistency; BF16 operands in the backward GEMMs"""
+    LAMBDA times the strength inconsistency; BF16 operands in the backward GEMMs
+    (the bias gradients are sums of the BF16-rounded dZ, as the tensor cores
+    form them); edges with a side shallower than WET carry no gradient"""
     P = unpack(p, np.float32 if rounding else np.float64)
     x, aux = features(*edges)
     o, I = forward(p, x, rounding)
@@ -148,7 +150,7 @@ def loss_and_grad(p, edges, targets, rounding=True):
     c, hm = aux["c"].astype(np.float64), aux["hm"].astype(np.float64)
     ish, ishu = 1.0 / (hm * c) ** 2, 1.0 / (hm * c * c) ** 2
     T = np.stack([np.asarray(t, dtype=np.float64) for t in targets], axis=1)
-    mask = (W["D"] >= TRAIN_SPREAD * c) & np.all(np.isfinite(W["U"]), axis=1)
+    mask = (aux["hmin"] >= WET) & (W["D"] >= TRAIN_SPREAD * c) & np.all(np.isfinite(W["U"]), axis=1)
     e = np.where(mask[:, None], W["U"] - T, 0.0)
     db1 = np.where(mask, W["bh1"] - W["b1"], 0.0)
     db2 = np.where(mask, W["bh2"] - W["b2"], 0.0)
@@ -176,16 +178,16 @@ def loss_and_grad(p, edges, targets, rounding=True):
         f32 = lambda a: a.astype(np.float32)
     g = {}
     dz4 = dO
-    g["b4"] = dz4.sum(0)
+    g["b4"] = f64(bf(dz4)).sum(0)
     g["W4"] = f64(bf(dz4)).T @ f64(I["a3"])
     dz3 = f32(f64(bf(dz4)) @ f64(bf(P["W4"]))) * f32(dsilu(f64(I["z3"])))
-    g["b3"] = dz3.sum(0)
+    g["b3"] = f64(bf(dz3)).sum(0)
     g["W3"] = f64(bf(dz3)).T @ f64(I["a2"])
     dz2 = f32(f64(bf(dz3)) @ f64(bf(P["W3"]))) * f32(dsilu(f64(I["z2"])))
-    g["b2"] = dz2.sum(0)
+    g["b2"] = f64(bf(dz2)).sum(0)
     g["W2"] = f64(bf(dz2)).T @ f64(I["a1"])
     dz1 = f32(f64(bf(dz2)) @ f64(bf(P["W2"]))) * f32(dsilu(f64(I["z1"])))
-    g["b1"] = dz1.sum(0)
+    g["b1"] = f64(bf(dz1)).sum(0)
     g["W1"] = f64(bf(dz1)).T @ f64(I["a0"])
     return float(loss), pack(g, np.float32 if rounding else np.float64)
 

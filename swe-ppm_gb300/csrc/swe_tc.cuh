@@ -10,6 +10,15 @@
 // byte offset).  One MMA consumes a K slice of 16: its descriptor starts
 // 256 bytes further per slice.
 //
+// The same bytes read as an MN-major operand (instruction-descriptor
+// transpose bit set): a matrix stored K-major with W columns serves as an
+// operand whose K runs over the stored ROWS and whose M or N runs over the
+// stored columns.  A core matrix is then 8 K-rows of 8 consecutive M/N
+// elements -- the same 128 bytes -- with M/N blocks 128 bytes apart and K
+// blocks (W/8) * 128 bytes apart.  So a buffer of activations [edge][neuron]
+// is both the A operand of the next layer's GEMM and, transposed for free, an
+// operand of the weight-gradient GEMM (K = edges).
+//
 // Accumulators: M = 128 rows, row r in TMEM lane r, column j in TMEM column
 // base + j (FP32).  Warp w of the CTA reads lanes 32w .. 32w+31.
 #pragma once
@@ -35,9 +44,21 @@ __device__ __forceinline__ uint64_t smemDesc(const void *base, int k0, int K) {
            (uint64_t((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);  // descriptor version of sm_100 family
 }
 
-/// instruction descriptor: BF16 A and B, FP32 D, both K-major, M x N
-__host__ __device__ constexpr uint32_t idescBf16(int M, int N) {
-    return (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(N >> 3) << 17) | (uint32_t(M >> 4) << 24);
+/// MN-major descriptor of the K slice starting at stored row k0 of a matrix
+/// stored K-major with W columns (see the layout note above)
+__device__ __forceinline__ uint64_t smemDescMN(const void *base, int k0, int W) {
+    const uint32_t kblock = uint32_t(W >> 3) * 128u;
+    const uint32_t addr = smemAddr(base) + uint32_t(k0 >> 3) * kblock;
+    const uint32_t lbo = kblock, sbo = 128u;
+    return uint64_t((addr >> 4) & 0x3FFFu) | (uint64_t((lbo >> 4) & 0x3FFFu) << 16) |
+           (uint64_t((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+/// instruction descriptor: BF16 A and B, FP32 D, M x N; aMN / bMN select
+/// the MN-major (transposed) reading of A / B
+__host__ __device__ constexpr uint32_t idescBf16(int M, int N, bool aMN = false, bool bMN = false) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(aMN) << 15) | (uint32_t(bMN) << 16) |
+           (uint32_t(N >> 3) << 17) | (uint32_t(M >> 4) << 24);
 }
 
 /// TMEM columns for the CTA (warp-wide; a power of two >= 32); the address lands in *slot

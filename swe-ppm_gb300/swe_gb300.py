@@ -45,7 +45,9 @@ EXPORTED = [
     "swe_gpu_launch_count", "swe_gpu_speed_pass_stats", "swe_gpu_lts_advance", "swe_gpu_lts_state", "swe_gpu_lts_blocks",
     "swe_gpu_block_steps", "swe_gpu_ensemble_create", "swe_gpu_group_count", "swe_gpu_group_state",
     "swe_gpu_retile", "swe_gpu_autotune",
-    "swe_mlp_last_error", "swe_mlp_gemm_check",
+    "swe_mlp_last_error", "swe_mlp_gemm_check", "swe_mlp_param_count", "swe_mlp_create", "swe_mlp_destroy",
+    "swe_mlp_get_params", "swe_mlp_set_params", "swe_mlp_forward", "swe_mlp_solve", "swe_mlp_loss_grad",
+    "swe_mlp_train",
     "swe_nc_open", "swe_nc_write_step", "swe_nc_write_step_slabs", "swe_nc_close",
     "swe_host_scenario_geometry", "swe_host_scenario_boundary", "swe_host_init_block", "swe_host_decompose",
 ]
@@ -111,7 +113,16 @@ def lib():
         L.swe_gpu_lts_blocks.argtypes = [vp, vp, vp]
         L.swe_gpu_block_steps.argtypes = [vp, vp]
         L.swe_mlp_last_error.restype = C.c_char_p
-        L.swe_mlp_gemm_check.argtypes = [C.c_int, C.c_int, vp, vp, vp]
+        L.swe_mlp_gemm_check.argtypes = [C.c_int, C.c_int, C.c_int, vp, vp, vp]
+        L.swe_mlp_create.argtypes = [C.c_ulonglong, C.POINTER(vp)]
+        L.swe_mlp_destroy.argtypes = [vp]
+        L.swe_mlp_destroy.restype = None
+        L.swe_mlp_get_params.argtypes = [vp, vp]
+        L.swe_mlp_set_params.argtypes = [vp, vp]
+        L.swe_mlp_forward.argtypes = [vp, C.c_int, vp, vp]
+        L.swe_mlp_solve.argtypes = [vp, C.c_int, vp, vp, vp, vp]
+        L.swe_mlp_loss_grad.argtypes = [vp, C.c_int, vp, vp, C.POINTER(C.c_float), vp]
+        L.swe_mlp_train.argtypes = [vp, C.c_int, vp, vp, C.c_int, C.c_int, C.c_float, C.c_ulonglong, vp]
         L.swe_gpu_ensemble_create.argtypes = [C.POINTER(Instance), C.c_int, C.POINTER(Desc), C.POINTER(vp)]
         L.swe_gpu_group_count.argtypes = [vp, C.POINTER(C.c_int)]
         L.swe_gpu_group_state.argtypes = [vp, vp, vp, vp]
@@ -448,13 +459,90 @@ def _mlp_check(rc):
         raise SweGpuError("swe_mlp error %d: %s" % (rc, lib().swe_mlp_last_error().decode()))
 
 
-def tc_gemm_check(a, b):
-    """D = A B^T on the tensor cores (BF16 in, FP32 out), A 128 x k, B n x k"""
-    a = np.ascontiguousarray(a, dtype=np.float32)
-    b = np.ascontiguousarray(b, dtype=np.float32)
-    d = np.zeros((128, b.shape[0]), dtype=np.float32)
-    _mlp_check(lib().swe_mlp_gemm_check(b.shape[0], a.shape[1], _p(a), _p(b), _p(d)))
+def tc_gemm_check(x, y, mode=0):
+    """Tensor-core GEMM of one CTA (BF16 in, FP32 out): mode 0 D = X Y^T
+    (X 128 x k, Y n x k), mode 1 D = X^T Y (X 128 x w1, Y 128 x w2; rows >= w1
+    undefined), mode 2 D = X Y (X 128 x w1, Y w1 x w2); D has 128 rows."""
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    y = np.ascontiguousarray(y, dtype=np.float32)
+    w1 = x.shape[1]
+    w2 = y.shape[0] if mode == 0 else y.shape[1]
+    d = np.zeros((128, w2), dtype=np.float32)
+    _mlp_check(lib().swe_mlp_gemm_check(int(mode), w1, w2, _p(x), _p(y), _p(d)))
     return d
+
+
+def _edges_soa(edges):
+    e = np.ascontiguousarray(edges, dtype=np.float32)
+    if e.ndim != 2 or e.shape[0] != 6:
+        raise ValueError("edges must be a 6 x n array (hL, hR, huL, huR, bL, bR)")
+    return e
+
+
+class Surrogate:
+    """MLP surrogate of the augmented Riemann solver (tensor-core forward,
+    backward and Adam training on the device)."""
+
+    NPARAMS = 9028
+
+    def __init__(self, seed=0):
+        self.h = C.c_void_p()
+        _mlp_check(lib().swe_mlp_create(int(seed), C.byref(self.h)))
+
+    def close(self):
+        if self.h:
+            lib().swe_mlp_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def params(self):
+        p = np.zeros(self.NPARAMS, np.float32)
+        _mlp_check(lib().swe_mlp_get_params(self.h, _p(p)))
+        return p
+
+    @params.setter
+    def params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        assert p.size == self.NPARAMS
+        _mlp_check(lib().swe_mlp_set_params(self.h, _p(p)))
+
+    def forward(self, edges):
+        e = _edges_soa(edges)
+        out = np.zeros((4, e.shape[1]), np.float32)
+        _mlp_check(lib().swe_mlp_forward(self.h, e.shape[1], _p(e), _p(out)))
+        return out
+
+    def solve(self, edges):
+        """net updates (4 x n), max wave speed (n), used-surrogate flags (n)"""
+        e = _edges_soa(edges)
+        n = e.shape[1]
+        upd = np.zeros((4, n), np.float32)
+        spd = np.zeros(n, np.float32)
+        used = np.zeros(n, np.uint8)
+        _mlp_check(lib().swe_mlp_solve(self.h, n, _p(e), _p(upd), _p(spd), _p(used)))
+        return upd, spd, used.astype(bool)
+
+    def loss_grad(self, edges, targets):
+        e = _edges_soa(edges)
+        t = np.ascontiguousarray(targets, dtype=np.float32)
+        g = np.zeros(self.NPARAMS, np.float32)
+        loss = C.c_float()
+        _mlp_check(lib().swe_mlp_loss_grad(self.h, e.shape[1], _p(e), _p(t), C.byref(loss), _p(g)))
+        return loss.value, g
+
+    def train(self, edges, targets, epochs, batch=4096, lr=1e-3, seed=0):
+        e = _edges_soa(edges)
+        t = np.ascontiguousarray(targets, dtype=np.float32)
+        losses = np.zeros(epochs, np.float32)
+        _mlp_check(lib().swe_mlp_train(self.h, e.shape[1], _p(e), _p(t), int(epochs), int(batch), float(lr), int(seed),
+                                       _p(losses)))
+        return losses
 
 
 def dam_break_ensemble(count, seed, sizes=None, length=1000.0):
