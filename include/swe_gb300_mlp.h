@@ -10,6 +10,8 @@
 #ifndef SWE_GB300_MLP_H
 #define SWE_GB300_MLP_H
 
+#include "swe_gb300.h"
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -58,6 +60,28 @@ int swe_mlp_loss_grad(swe_mlp *m, int n, const float *edges, const float *target
  * mean loss of each epoch, measured during the pass. */
 int swe_mlp_train(swe_mlp *m, int n, const float *edges, const float *targets, int epochs, int batch, float lr,
                   unsigned long long seed, float *epoch_loss);
+
+/* The surrogate on a domain of swe_gb300.h (unsplit semantics, no local time
+ * stepping).  Each of the nsteps steps runs setGhostLayer, an edge pass that
+ * stores the net updates of every edge (the surrogate where its gate accepts,
+ * the augmented Riemann solver elsewhere), the dt of each dt group from the
+ * max wave speed (src/blocks/SWE_DimensionalSplittingMpi.cpp:448-456) and the
+ * unsplit cell update (:458-492).  m == NULL runs the augmented solver on every
+ * edge through the same kernels: bit-identical to steps of a domain created
+ * with SWE_SOLVER_AUGRIE.  Steps do not stop at an advance target.
+ * *surrogate_edges (may be NULL; the call then waits) counts the edges the
+ * surrogate solved over the call.  Allocates the edge buffers (8 floats per
+ * cell) on first use. */
+int swe_gpu_surrogate_step(swe_gpu_domain *d, swe_mlp *m, int nsteps, long long *surrogate_edges);
+/* Edges one step solves: x-edges (nx+1) ny plus y-edges nx (ny+1), all blocks. */
+int swe_gpu_surrogate_edge_count(swe_gpu_domain *d, long long *edges);
+
+/* Edge-state logger: after setGhostLayer of the current state, every
+ * stride-th edge of the step's edge order with both sides at least 0.1 m deep
+ * (up to capacity of them, in edge order) with its augmented-solver net
+ * updates: edges 6 x capacity, targets 4 x capacity (row stride capacity),
+ * *count of them filled -- training data for swe_mlp_train. */
+int swe_gpu_log_edges(swe_gpu_domain *d, int stride, int capacity, float *edges, float *targets, int *count);
 
 /* Tensor-core self-check, one CTA, host arrays (row-major), operands rounded
  * to BF16, FP32 accumulation:

@@ -12,8 +12,10 @@
 #include <vector>
 
 #include "../../include/swe_gb300.h"
+#include "../../include/swe_gb300_mlp.h"
 #include "swe_device.cuh"
 #include "swe_launch.hpp"
+#include "swe_mlp_launch.hpp"
 
 
 using namespace swegb;
@@ -265,6 +267,11 @@ struct swe_gpu_domain {
     long long ringElems = 0;
     cudaGraphExec_t ltsGraph = nullptr;
     long long ltsGraphKernels = 0;
+    // surrogate step and edge logger: edge tiles and the stored net updates
+    std::vector<mlp::EdgeTile> edgeTiles;
+    mlp::EdgeTile *dEdgeTiles = nullptr;
+    float *edgeBuf = nullptr;             // 8 fields: x-edge then y-edge net updates
+    unsigned long long *dUsed = nullptr;  // edges the surrogate solved
 };
 
 namespace {
@@ -366,6 +373,9 @@ void freeDomain(swe_gpu_domain *D) {
     cudaFree(D->dTiles);
     cudaFree(D->dTileW);
     cudaFree(D->dTileKey);
+    cudaFree(D->dEdgeTiles);
+    cudaFree(D->edgeBuf);
+    cudaFree(D->dUsed);
     if (D->ownStream) cudaStreamDestroy(D->ownStream);
     delete D;
 }
@@ -1439,6 +1449,98 @@ int swe_gpu_solve_edges(int solver, long long n, const float *hL, const float *h
     default: return fail(SWE_GPU_ERR_INVALID, "unknown solver %d", solver);
     }
     CUDA_TRY(cudaGetLastError());
+    return SWE_GPU_OK;
+}
+
+
+// ---------------------------------------------------------------------------
+// MLP surrogate on a domain (include/swe_gb300_mlp.h)
+// ---------------------------------------------------------------------------
+static int ensureEdgeTiles(swe_gpu_domain *D) {
+    if (D->dEdgeTiles) return SWE_GPU_OK;
+    D->edgeTiles = mlp::buildEdgeTiles(D->blocks);
+    CUDA_TRY(cudaMalloc(&D->dEdgeTiles, D->edgeTiles.size() * sizeof(mlp::EdgeTile)));
+    CUDA_TRY(cudaMemcpy(D->dEdgeTiles, D->edgeTiles.data(), D->edgeTiles.size() * sizeof(mlp::EdgeTile),
+                        cudaMemcpyHostToDevice));
+    return SWE_GPU_OK;
+}
+
+int swe_gpu_surrogate_step(swe_gpu_domain *dom, swe_mlp *m, int nsteps, long long *surrogate_edges) {
+    if (!dom || nsteps < 0) return fail(SWE_GPU_ERR_INVALID, "bad argument");
+    if (dom->lts) return fail(SWE_GPU_ERR_INVALID, "local-time-stepping domain: the surrogate step is global");
+    if (dom->semantics != SEM_UNSPLIT) return fail(SWE_GPU_ERR_INVALID, "the surrogate step is the unsplit step (semantics 0)");
+    CUDA_TRY(cudaSetDevice(dom->device));
+    int rc = ensureEdgeTiles(dom);
+    if (rc) return rc;
+    if (!dom->edgeBuf) CUDA_TRY(cudaMalloc(&dom->edgeBuf, 8 * dom->fieldElems * sizeof(float)));
+    if (!dom->dUsed) CUDA_TRY(cudaMalloc(&dom->dUsed, sizeof(unsigned long long)));
+    mlp::EdgeUpdates u;
+    for (int k = 0; k < 4; k++) {
+        u.x[k] = dom->edgeBuf + size_t(k) * dom->fieldElems;
+        u.y[k] = dom->edgeBuf + size_t(4 + k) * dom->fieldElems;
+    }
+    long long maxCells = 0;
+    for (const BlockDesc &B : dom->blocks) maxCells = std::max(maxCells, (long long)B.nx * B.ny);
+    CUDA_TRY(cudaMemsetAsync(dom->dUsed, 0, sizeof(unsigned long long), dom->stream));
+    const int ntiles = int(dom->edgeTiles.size());
+    for (int i = 0; i < nsteps; i++) {
+        if ((rc = enqueueGhost(dom, 0))) return rc;
+        CUDA_TRY(mlp::launchSurrogateEdges(dom->dev, m, dom->dEdgeTiles, ntiles, u, dom->dUsed, dom->stream));
+        CUDA_TRY(mlp::launchSurrogateDt(dom->dev, dom->ngroups, dom->stream));
+        CUDA_TRY(mlp::launchSurrogateApply(dom->dev, u, int(dom->blocks.size()), maxCells, dom->stream));
+        CUDA_TRY(mlp::launchSurrogateFinish(dom->dev, dom->ngroups, dom->stream));
+        dom->launches += 4;
+    }
+    dom->ghostsValid = false;
+    if (surrogate_edges) {
+        unsigned long long used = 0;
+        CUDA_TRY(cudaStreamSynchronize(dom->stream));
+        CUDA_TRY(cudaMemcpy(&used, dom->dUsed, sizeof(used), cudaMemcpyDeviceToHost));
+        *surrogate_edges = (long long)used;
+    }
+    if (m) {
+        CUDA_TRY(cudaStreamSynchronize(dom->stream));
+        if (mlp::checkDeviceError(m, "surrogate step")) return fail(SWE_GPU_ERR_DEVICE, "%s", swe_mlp_last_error());
+    }
+    return SWE_GPU_OK;
+}
+
+int swe_gpu_surrogate_edge_count(swe_gpu_domain *dom, long long *edges) {
+    if (!dom || !edges) return fail(SWE_GPU_ERR_INVALID, "null argument");
+    long long n = 0;
+    for (const BlockDesc &B : dom->blocks) n += (long long)(B.nx + 1) * B.ny + (long long)B.nx * (B.ny + 1);
+    *edges = n;
+    return SWE_GPU_OK;
+}
+
+int swe_gpu_log_edges(swe_gpu_domain *dom, int stride, int capacity, float *edges, float *targets, int *count) {
+    if (!dom || stride < 1 || capacity < 0 || !count || (capacity > 0 && (!edges || !targets)))
+        return fail(SWE_GPU_ERR_INVALID, "bad argument");
+    if (dom->lts) return fail(SWE_GPU_ERR_INVALID, "local-time-stepping domain");
+    CUDA_TRY(cudaSetDevice(dom->device));
+    int rc = ensureEdgeTiles(dom);
+    if (rc) return rc;
+    if ((rc = enqueueGhost(dom, 0))) return rc;
+    dom->ghostsValid = true;
+    const int ntiles = int(dom->edgeTiles.size());
+    const long long nslots = ((long long)ntiles * 128 + stride - 1) / stride;
+    float *dSlots = nullptr;
+    CUDA_TRY(cudaMalloc(&dSlots, size_t(11) * nslots * sizeof(float)));
+    std::vector<float> hs(size_t(11) * nslots);
+    cudaError_t e = mlp::launchLogEdges(dom->dev, dom->dEdgeTiles, ntiles, stride, dSlots, nslots, dom->stream);
+    dom->launches++;
+    if (e == cudaSuccess) e = cudaStreamSynchronize(dom->stream);
+    if (e == cudaSuccess) e = cudaMemcpy(hs.data(), dSlots, hs.size() * sizeof(float), cudaMemcpyDeviceToHost);
+    cudaFree(dSlots);
+    if (e != cudaSuccess) return fail(SWE_GPU_ERR_CUDA, "log edges: %s", cudaGetErrorString(e));
+    int c = 0;
+    for (long long k = 0; k < nslots && c < capacity; k++) {
+        if (hs[size_t(10) * nslots + k] == 0.f) continue;
+        for (int f = 0; f < 6; f++) edges[size_t(f) * capacity + c] = hs[size_t(f) * nslots + k];
+        for (int f = 0; f < 4; f++) targets[size_t(f) * capacity + c] = hs[size_t(6 + f) * nslots + k];
+        c++;
+    }
+    *count = c;
     return SWE_GPU_OK;
 }
 

@@ -34,6 +34,8 @@
 #include "../../include/swe_gb300.h"
 #include "../../include/swe_gb300_mlp.h"
 #include "swe_device.cuh"
+#include "swe_mlp_launch.hpp"
+#include "swe_sweep.cuh"
 #include "swe_tc.cuh"
 
 namespace swegb {
@@ -642,6 +644,218 @@ __global__ void __launch_bounds__(128) gemmCheckKernel(int mode, const __nv_bflo
     if (t < 32) tc::tmemFree(taddr, 128);
 }
 
+
+// ---------------------------------------------------------------------------
+// surrogate step of a domain: edge pass, dt, cell update, finish
+// ---------------------------------------------------------------------------
+/// the six edge inputs of edge (tile, t) in the current buffer; false past the tile's end
+__device__ __forceinline__ bool loadDomainEdge(const DomainDev &d, const EdgeTile &T, const BlockDesc &B, int cur, int t,
+                                               float q[6], long long &oL) {
+    const long long P = B.pitch;
+    oL = B.base + (long long)T.col * P + (T.j0 + t);
+    if (t >= T.count) return false;
+    const long long oR = T.dir ? oL + 1 : oL + P;
+    const float *H = pick(d.h, cur);
+    const float *N = T.dir ? pick(d.hv, cur) : pick(d.hu, cur);
+    q[0] = H[oL];
+    q[1] = H[oR];
+    q[2] = N[oL];
+    q[3] = N[oR];
+    q[4] = d.b[oL];
+    q[5] = d.b[oR];
+    return true;
+}
+
+/// the CTA's running max wave speed goes to its group
+__device__ __forceinline__ void flushSpeed(const DomainDev &d, int group, float &smax, float *sMax) {
+    float v = smax;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = vmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if ((threadIdx.x & 31) == 0) sMax[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const float m = vmax(vmax(sMax[0], sMax[1]), vmax(sMax[2], sMax[3]));
+        atomicMax(&d.groups[group].speedBits, __float_as_uint(m));
+    }
+    __syncthreads();
+    smax = 0.f;
+}
+
+/// edge pass over a contiguous range of tiles per CTA (so the group changes
+/// rarely within a CTA).  SURR: surrogate with the gate, else the augmented
+/// solver on every edge.
+template <bool SURR>
+__global__ void __launch_bounds__(128) surrogateEdgeKernel(const DomainDev d, const uint8_t *image, const EdgeTile *tiles,
+                                                           int ntiles, EdgeUpdates u, unsigned long long *usedCount,
+                                                           int *err) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tslot;
+    __shared__ float sMax[4];
+    const int t = threadIdx.x;
+    uint8_t *sW = smem, *sX0 = smem + kFwdX0, *sAct = smem + kFwdAct;
+    uint32_t tm = 0;
+    if (SURR) {
+        stageImage(image, sW);
+        if (t == 0) tc::mbarInit(&mbar, 1);
+        if (t < 32) tc::tmemAlloc(&tslot, kFwdCols);
+        tc::fenceBeforeSync();
+        __syncthreads();
+        tc::fenceAfterSync();
+        tm = tslot;
+    }
+    const float *bias = reinterpret_cast<const float *>(sW + pBias);
+    uint8_t *const act[3] = {sAct, sAct, sAct};
+    const uint32_t zc[3] = {0, 0, 0};
+    uint32_t phase = 0;
+    bool ok = true;
+    float smax = 0.f;
+    unsigned usedLocal = 0;
+    const int first = int((long long)ntiles * blockIdx.x / gridDim.x);
+    const int last = int((long long)ntiles * (blockIdx.x + 1) / gridDim.x);
+    int group = -1;
+    for (int tile = first; tile < last; tile++) {
+        const EdgeTile T = tiles[tile];
+        const BlockDesc &B = d.blocks[T.block];
+        if (B.group != group) {
+            if (group >= 0) flushSpeed(d, group, smax, sMax);
+            group = B.group;
+        }
+        const int cur = d.groups[group].cur;
+        float q[6] = {1.f, 1.f, 0.f, 0.f, 0.f, 0.f};
+        long long oL;
+        const bool valid = loadDomainEdge(d, T, B, cur, t, q, oL);
+        float upd[4], s = 0.f;
+        bool use = false;
+        if (SURR) {
+            EdgeFeat f;
+            edgeFeatures(q[0], q[1], q[2], q[3], q[4], q[5], f);
+            storeX0(sX0, t, f.x);
+            if (!(ok = forwardTile(tm, sW, sX0, act, zc, 0, &mbar, phase))) break;
+            float v[16];
+            tc::load16(tm, 0, v);
+            float o[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++) o[k] = v[k] + bias[3 * kHid + k];
+            Waves w;
+            surrogateWaves(o, f, w);
+            use = valid && surrogateGate(f, w);
+            if (use) {
+#pragma unroll
+                for (int k = 0; k < 4; k++) upd[k] = w.U[k];
+                s = fmaxf(fabsf(w.s1), fabsf(w.s2));
+            }
+        }
+        if (valid) {
+            if (!use) edgeAugRie(q[0], q[1], q[2], q[3], q[4], q[5], upd[0], upd[1], upd[2], upd[3], s);
+            float *const *dst = T.dir ? u.y : u.x;
+#pragma unroll
+            for (int k = 0; k < 4; k++) dst[k][oL] = upd[k];
+            smax = vmax(smax, s);
+            usedLocal += use ? 1u : 0u;
+        }
+    }
+    if (ok && group >= 0) flushSpeed(d, group, smax, sMax);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) usedLocal += __shfl_xor_sync(0xffffffffu, usedLocal, o);
+    if ((t & 31) == 0 && usedLocal) atomicAdd(usedCount, (unsigned long long)usedLocal);
+    if (SURR) {
+        if (!ok) {
+            if (t == 0) atomicOr(err, 1);
+            tc::mbarWait(&mbar, phase);  // bounded
+        }
+        tc::fenceBeforeSync();
+        __syncthreads();
+        if (t < 32) tc::tmemFree(tm, kFwdCols);
+    }
+}
+
+/// maxTimestep of every group from the edge pass's max wave speed
+/// (src/blocks/SWE_DimensionalSplittingMpi.cpp:448-456)
+__global__ void surrogateDtKernel(const DomainDev d, int ngroups) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= ngroups) return;
+    GroupState *G = d.groups + g;
+    const float s = __uint_as_float(G->speedBits);
+    const BlockDesc &F = d.blocks[G->firstBlock];
+    G->speed = s;
+    G->dt = timestepFromSpeed(s, F.dx, F.dy, SEM_UNSPLIT);
+    if (!(s == s)) G->status |= 1;
+    G->speedBits = 0u;
+}
+
+/// the unsplit cell update (src/blocks/SWE_DimensionalSplittingMpi.cpp:458-492)
+/// from the stored net updates: Q^{n+1} of interior cell (i, j) into the other buffer
+__global__ void surrogateApplyKernel(const DomainDev d, EdgeUpdates u) {
+    const BlockDesc B = d.blocks[blockIdx.y];
+    GroupState *G = d.groups + B.group;
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)B.nx * B.ny) return;
+    const int i = int(idx / B.ny) + 1, j = int(idx % B.ny) + 1;
+    const int cur = G->cur;
+    const float dt = G->dt;
+    const float dtdx = dt / B.dx, dtdy = dt / B.dy;
+    const long long P = B.pitch;
+    const long long o = B.base + (long long)i * P + j;
+    const float sxH = u.x[1][o - P] + u.x[0][o];
+    const float sxHU = u.x[3][o - P] + u.x[2][o];
+    const float syH = u.y[1][o - 1] + u.y[0][o];
+    const float syHV = u.y[3][o - 1] + u.y[2][o];
+    float hn = pick(d.h, cur)[o] - (dtdx * sxH + dtdy * syH);
+    float hun = pick(d.hu, cur)[o] - dtdx * sxHU;
+    float hvn = pick(d.hv, cur)[o] - dtdy * syHV;
+    if (hn < 0.f) {
+        hn = 0.f; hun = 0.f; hvn = 0.f;
+    } else if (hn < 0.1f) {
+        hun = 0.f; hvn = 0.f;
+    }
+    pick(d.h, cur ^ 1)[o] = hn;
+    pick(d.hu, cur ^ 1)[o] = hun;
+    pick(d.hv, cur ^ 1)[o] = hvn;
+    if (!(fabsf(hn) <= FLT_MAX)) atomicOr(&G->status, 2);
+}
+
+__global__ void surrogateFinishKernel(const DomainDev d, int ngroups) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= ngroups) return;
+    GroupState *G = d.groups + g;
+    G->time = G->time + G->dt;
+    G->steps = G->steps + 1;
+    G->cur = G->cur ^ 1;
+    G->ghostsAhead = 0;  // the new buffer's ghost ring is stale
+    G->boundsValid[0] = 0;
+    G->boundsValid[1] = 0;
+}
+
+/// edge-state logger: inputs and augmented-solver net updates of every
+/// stride-th edge into fixed slots (deterministic, whatever the launch shape)
+__global__ void logEdgesKernel(const DomainDev d, const EdgeTile *tiles, int ntiles, int stride, float *slots,
+                               long long nslots) {
+    const int tile = blockIdx.x;
+    if (tile >= ntiles) return;
+    const long long e = (long long)tile * kTile + threadIdx.x;
+    if (e % stride) return;
+    const long long slot = e / stride;
+    if (slot >= nslots) return;
+    const EdgeTile T = tiles[tile];
+    const BlockDesc &B = d.blocks[T.block];
+    const int cur = d.groups[B.group].cur;
+    float q[6];
+    long long oL;
+    float wet = 0.f;
+    float r[4] = {0.f, 0.f, 0.f, 0.f};
+    if (loadDomainEdge(d, T, B, cur, threadIdx.x, q, oL)) {
+        float s;
+        edgeAugRie(q[0], q[1], q[2], q[3], q[4], q[5], r[0], r[1], r[2], r[3], s);
+        wet = (q[0] >= kWet && q[1] >= kWet) ? 1.f : 0.f;
+    } else {
+        for (int k = 0; k < 6; k++) q[k] = 0.f;
+    }
+    for (int k = 0; k < 6; k++) slots[k * nslots + slot] = q[k];
+    for (int k = 0; k < 4; k++) slots[(6 + k) * nslots + slot] = r[k];
+    slots[10 * nslots + slot] = wet;
+}
+
 } // namespace mlp
 } // namespace swegb
 
@@ -985,3 +1199,53 @@ int swe_mlp_gemm_check(int mode, int w1, int w2, const float *x, const float *y,
 }
 
 } // extern "C"
+
+// ---------------------------------------------------------------------------
+// launchers of the domain kernels (swe_mlp_launch.hpp)
+// ---------------------------------------------------------------------------
+namespace swegb {
+namespace mlp {
+
+cudaError_t launchSurrogateEdges(const DomainDev &d, const swe_mlp *m, const EdgeTile *tiles, int ntiles, EdgeUpdates u,
+                                 unsigned long long *used, cudaStream_t s) {
+    if (ntiles <= 0) return cudaSuccess;
+    if (m) {
+        const int grid = std::min(ntiles, m->sms * m->fwdBlocksPerSm);
+        surrogateEdgeKernel<true><<<grid, 128, kFwdSmem, s>>>(d, m->image, tiles, ntiles, u, used, m->err);
+    } else {
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        const int grid = std::min(ntiles, sms * 8);
+        surrogateEdgeKernel<false><<<grid, 128, 0, s>>>(d, nullptr, tiles, ntiles, u, used, nullptr);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launchSurrogateDt(const DomainDev &d, int ngroups, cudaStream_t s) {
+    surrogateDtKernel<<<(ngroups + 127) / 128, 128, 0, s>>>(d, ngroups);
+    return cudaGetLastError();
+}
+
+cudaError_t launchSurrogateApply(const DomainDev &d, EdgeUpdates u, int nblocks, long long maxCells, cudaStream_t s) {
+    const dim3 grid(unsigned((maxCells + 255) / 256), unsigned(nblocks));
+    surrogateApplyKernel<<<grid, 256, 0, s>>>(d, u);
+    return cudaGetLastError();
+}
+
+cudaError_t launchSurrogateFinish(const DomainDev &d, int ngroups, cudaStream_t s) {
+    surrogateFinishKernel<<<(ngroups + 127) / 128, 128, 0, s>>>(d, ngroups);
+    return cudaGetLastError();
+}
+
+cudaError_t launchLogEdges(const DomainDev &d, const EdgeTile *tiles, int ntiles, int stride, float *slots,
+                           long long nslots, cudaStream_t s) {
+    if (ntiles <= 0) return cudaSuccess;
+    logEdgesKernel<<<ntiles, kTile, 0, s>>>(d, tiles, ntiles, stride, slots, nslots);
+    return cudaGetLastError();
+}
+
+int checkDeviceError(swe_mlp *m, const char *what) { return m ? m->checkErr(what) : SWE_GPU_OK; }
+
+} // namespace mlp
+} // namespace swegb

@@ -47,7 +47,7 @@ EXPORTED = [
     "swe_gpu_retile", "swe_gpu_autotune",
     "swe_mlp_last_error", "swe_mlp_gemm_check", "swe_mlp_param_count", "swe_mlp_create", "swe_mlp_destroy",
     "swe_mlp_get_params", "swe_mlp_set_params", "swe_mlp_forward", "swe_mlp_solve", "swe_mlp_loss_grad",
-    "swe_mlp_train",
+    "swe_mlp_train", "swe_gpu_surrogate_step", "swe_gpu_surrogate_edge_count", "swe_gpu_log_edges",
     "swe_nc_open", "swe_nc_write_step", "swe_nc_write_step_slabs", "swe_nc_close",
     "swe_host_scenario_geometry", "swe_host_scenario_boundary", "swe_host_init_block", "swe_host_decompose",
 ]
@@ -123,6 +123,9 @@ def lib():
         L.swe_mlp_solve.argtypes = [vp, C.c_int, vp, vp, vp, vp]
         L.swe_mlp_loss_grad.argtypes = [vp, C.c_int, vp, vp, C.POINTER(C.c_float), vp]
         L.swe_mlp_train.argtypes = [vp, C.c_int, vp, vp, C.c_int, C.c_int, C.c_float, C.c_ulonglong, vp]
+        L.swe_gpu_surrogate_step.argtypes = [vp, vp, C.c_int, C.POINTER(C.c_longlong)]
+        L.swe_gpu_surrogate_edge_count.argtypes = [vp, C.POINTER(C.c_longlong)]
+        L.swe_gpu_log_edges.argtypes = [vp, C.c_int, C.c_int, vp, vp, C.POINTER(C.c_int)]
         L.swe_gpu_ensemble_create.argtypes = [C.POINTER(Instance), C.c_int, C.POINTER(Desc), C.POINTER(vp)]
         L.swe_gpu_group_count.argtypes = [vp, C.POINTER(C.c_int)]
         L.swe_gpu_group_state.argtypes = [vp, vp, vp, vp]
@@ -378,6 +381,29 @@ class Domain:
         r, c, ms = C.c_int(), C.c_int(), C.c_float()
         _check(lib().swe_gpu_autotune(self.handle, int(trial_steps), C.byref(r), C.byref(c), C.byref(ms)))
         return r.value, c.value, ms.value
+
+    def surrogate_step(self, surrogate, nsteps=1, count=True):
+        """nsteps unsplit steps with the MLP surrogate (a Surrogate; None: the
+        augmented solver on every edge through the same kernels); returns the
+        number of edges the surrogate solved when count is set"""
+        used = C.c_longlong()
+        _check(lib().swe_gpu_surrogate_step(self.handle, surrogate.h if surrogate is not None else None, int(nsteps),
+                                            C.byref(used) if count else None))
+        return used.value if count else None
+
+    def surrogate_edge_count(self):
+        n = C.c_longlong()
+        _check(lib().swe_gpu_surrogate_edge_count(self.handle, C.byref(n)))
+        return n.value
+
+    def log_edges(self, stride=1, capacity=1 << 20):
+        """wet edge states of the current state and their augmented-solver net
+        updates: (edges 6 x count, targets 4 x count)"""
+        e = np.zeros((6, capacity), np.float32)
+        t = np.zeros((4, capacity), np.float32)
+        c = C.c_int()
+        _check(lib().swe_gpu_log_edges(self.handle, int(stride), int(capacity), _p(e), _p(t), C.byref(c)))
+        return e[:, :c.value].copy(), t[:, :c.value].copy()
 
     def block_steps(self):
         """update steps each block has executed"""

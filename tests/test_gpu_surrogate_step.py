@@ -1,0 +1,112 @@
+"""The MLP surrogate on a domain: the edge-buffer step with the augmented
+solver on every edge must equal the augmented solver's own step bit for bit
+(so the edge tiling, the stored net updates, dt and the cell update are
+exact); the edge-state logger must log the step's edge states with the
+oracle's augmented-solver net updates; a surrogate trained on logged edges
+must stay closer to the augmented solver's run than the f-wave solver does."""
+import numpy as np
+import pytest
+
+from helpers import assert_bitwise
+
+pytestmark = pytest.mark.gpu
+
+
+def make(swe, geo, st, solver):
+    D = swe.Domain(geo["nx_cols"], geo["ny_rows"], geo["dx"], geo["dy"], boundary=geo["boundary"], solver=solver)
+    D.upload(*st)
+    D.exchange_bathymetry()
+    return D
+
+
+CASES = [
+    ("radial_dam_break", 0, 160, 128, 4, None),
+    ("half_domain_dry", 3, 96, 80, 1, None),
+    ("shoreline", 12, 192, 192, 4, [5.0, 50000.0]),
+    ("tsunami", 11, 256, 256, 4, [256, 7.0, 100000.0]),
+]
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
+def test_augmented_solver_through_edge_buffers_is_bitwise(swe, case):
+    name, sid, nx, ny, nb, params = case
+    geo, h, hu, hv, b = swe.init_domain(sid, nx, ny, nb, params)
+    st = (h, hu, hv, b)
+    A = make(swe, geo, st, swe.AUGRIE)
+    A.step(12)
+    ref = A.download()
+    tref, nref = A.time()
+    A.close()
+    S = make(swe, geo, st, swe.AUGRIE)
+    used = S.surrogate_step(None, 7)
+    S.step(5)  # regular steps continue from the surrogate path's state
+    out = S.download()
+    t, n = S.time()
+    assert S.status() == 0
+    S.close()
+    assert used == 0 and n == nref == 12
+    assert np.float32(t) == np.float32(tref)
+    for a, r, k in zip(out, ref, "h hu hv b".split()):
+        assert_bitwise(a, r, k)
+
+
+def test_log_edges_matches_oracle(swe, oracle_mod):
+    geo, h, hu, hv, b = swe.init_domain(11, 128, 96, 1, [128, 7.0, 100000.0])
+    D = make(swe, geo, (h, hu, hv, b), swe.AUGRIE)
+    D.step(3)
+    n_all = D.surrogate_edge_count()
+    assert n_all == 129 * 96 + 128 * 97
+    e1, t1 = D.log_edges(stride=1, capacity=1 << 20)
+    e7, t7 = D.log_edges(stride=7, capacity=1000)
+    st = D.download()
+    D.close()
+    assert e1.shape[1] == n_all  # the tsunami basin is wet everywhere
+    ref = oracle_mod.solve_edges(2, *e1)
+    for k in range(4):
+        assert_bitwise(t1[k], ref[k], "target %d" % k)
+    # the first tile: x-edges (0|1) of rows 1..96, from the state after setGhostLayer
+    H = st[0].reshape(130, 98)
+    assert_bitwise(e1[1, :96], H[1, 1:97], "right cells")
+    assert_bitwise(e1[0, :96], H[0, 1:97], "left ghosts (outflow copies)")
+    assert_bitwise(H[0, 1:97], H[1, 1:97], "outflow ghost")
+    # stride: every 7th slot of the padded tile order, capacity honoured
+    assert e7.shape[1] == 1000
+    assert np.isin(e7[0], e1[0]).all()
+
+
+def test_trained_surrogate_beats_the_f_wave_solver_on_a_shoreline(swe):
+    """Train on edges logged from an augmented-solver run of a shoreline
+    (Gaussian hump over a ramp onto dry land), then run the same start state
+    with the surrogate, with the augmented solver and with the f-wave solver:
+    the surrogate's water heights stay closer to the augmented solver's."""
+    n, nb = 192, 4
+    geo, h, hu, hv, b = swe.init_domain(12, n, n, nb, [5.0, 20000.0])
+    st = (h, hu, hv, b)
+    A = make(swe, geo, st, swe.AUGRIE)
+    E, T = [], []
+    for _ in range(6):
+        A.step(15)
+        e, t = A.log_edges(stride=3, capacity=1 << 18)
+        E.append(e)
+        T.append(t)
+    A.close()
+    E, T = np.concatenate(E, axis=1), np.concatenate(T, axis=1)
+    m = swe.Surrogate(seed=4)
+    losses = m.train(E, T, epochs=40, batch=4096, lr=2e-3, seed=5)
+    assert losses[-1] < losses[0]
+    steps = 60
+    runs = {}
+    for name, solver in (("aug", swe.AUGRIE), ("fwave", swe.FWAVE), ("sur", swe.AUGRIE)):
+        D = make(swe, geo, st, solver)
+        if name == "sur":
+            used = D.surrogate_step(m, steps)
+            frac = used / (steps * D.surrogate_edge_count())
+        else:
+            D.step(steps)
+        runs[name] = D.download()[0]
+        assert D.status() == 0
+        D.close()
+    m.close()
+    assert frac > 0.3, frac
+    err = lambda k: float(np.abs(runs[k] - runs["aug"]).sum())
+    assert err("sur") < err("fwave"), (err("sur"), err("fwave"), frac)
