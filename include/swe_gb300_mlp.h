@@ -66,7 +66,8 @@ int swe_mlp_train(swe_mlp *m, int n, const float *edges, const float *targets, i
  * stores the net updates of every edge (the surrogate where its gate accepts,
  * the augmented Riemann solver elsewhere), the dt of each dt group from the
  * max wave speed (src/blocks/SWE_DimensionalSplittingMpi.cpp:448-456) and the
- * unsplit cell update (:458-492).  m == NULL runs the augmented solver on every
+ * unsplit cell update (:458-492); the call ends with setGhostLayer of the
+ * new state, as a regular step leaves it.  m == NULL runs the augmented solver on every
  * edge through the same kernels: bit-identical to steps of a domain created
  * with SWE_SOLVER_AUGRIE.  Steps do not stop at an advance target.
  * *surrogate_edges (may be NULL; the call then waits) counts the edges the

@@ -1484,14 +1484,20 @@ int swe_gpu_surrogate_step(swe_gpu_domain *dom, swe_mlp *m, int nsteps, long lon
     CUDA_TRY(cudaMemsetAsync(dom->dUsed, 0, sizeof(unsigned long long), dom->stream));
     const int ntiles = int(dom->edgeTiles.size());
     for (int i = 0; i < nsteps; i++) {
-        if ((rc = enqueueGhost(dom, 0))) return rc;
+        if (i > 0 || !dom->ghostsValid) {
+            if ((rc = enqueueGhost(dom, 0))) return rc;
+        }
         CUDA_TRY(mlp::launchSurrogateEdges(dom->dev, m, dom->dEdgeTiles, ntiles, u, dom->dUsed, dom->stream));
         CUDA_TRY(mlp::launchSurrogateDt(dom->dev, dom->ngroups, dom->stream));
         CUDA_TRY(mlp::launchSurrogateApply(dom->dev, u, int(dom->blocks.size()), maxCells, dom->stream));
         CUDA_TRY(mlp::launchSurrogateFinish(dom->dev, dom->ngroups, dom->stream));
         dom->launches += 4;
     }
-    dom->ghostsValid = false;
+    // the ghost ring of the new state, as the regular update pass leaves it
+    if (nsteps > 0) {
+        if ((rc = enqueueGhost(dom, 0))) return rc;
+    }
+    dom->ghostsValid = true;
     if (surrogate_edges) {
         unsigned long long used = 0;
         CUDA_TRY(cudaStreamSynchronize(dom->stream));
