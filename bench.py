@@ -288,6 +288,117 @@ def ensemble_measure(swe, device, steps=100, count=256):
             "cells": int(cells.sum()), "ms": ms, "tile_rows": rows, "tile_cols": cols}
 
 
+def surrogate_measure(swe, device, steps=10, err_steps=120):
+    """MLP surrogate of the augmented Riemann solver at 4096^2: the shoreline
+    ramp (bathymetry -4000 m to +50 m across 50 km, seeded Gaussian bump) as
+    4x4 blocks of 1024^2, unsplit.  Training data: every 64th wet edge logged
+    at steps 10, 20, 30, 40 of an augmented-solver run; 8 epochs of Adam on the
+    device.  Timed (CUDA events, `steps` steps after warm-up): the augmented
+    solver's own step, the same solver through the edge-buffer step, and the
+    surrogate step.  Accuracy: each solver runs `err_steps` steps from the
+    start state with its own dt; the L1 distance of its water heights to the
+    augmented solver's trajectory, interpolated to the same time."""
+    import torch
+    n, nb = 4096, 16
+    geo, h, hu, hv, b = swe.init_domain(swe.SCENARIO_SHORELINE, n, n, nb, [SEED, 50000.0])
+    st = (h, hu, hv, b)
+    stream = torch.cuda.Stream()
+
+    def make(solver):
+        D = swe.Domain(geo["nx_cols"], geo["ny_rows"], geo["dx"], geo["dy"], boundary=geo["boundary"], solver=solver,
+                       device=device)
+        D.set_stream(stream.cuda_stream)
+        D.upload(*st)
+        D.exchange_bathymetry()
+        return D
+
+    A = make(swe.AUGRIE)
+    E, T = [], []
+    for _ in range(4):
+        A.step(10)
+        e, t = A.log_edges(stride=64, capacity=1 << 21)
+        E.append(e)
+        T.append(t)
+    A.close()
+    E, T = np.concatenate(E, axis=1), np.concatenate(T, axis=1)
+    m = swe.Surrogate(seed=SEED)
+    epochs = 8
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    losses = m.train(E, T, epochs=epochs, batch=8192, lr=2e-3, seed=SEED)
+    train_s = time.perf_counter() - t0
+
+    def timed(D, fn):
+        fn(D, 3)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            fn(D, steps)
+            e1.record(stream)
+        stream.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    cells = float(n * n)
+    rates = {}
+    D = make(swe.AUGRIE)
+    rates["augmented_step"] = cells / (1e-3 * timed(D, lambda D, k: D.step(k)))
+    D.close()
+    D = make(swe.AUGRIE)
+    rates["augmented_edge_buffer_step"] = cells / (1e-3 * timed(D, lambda D, k: D.surrogate_step(None, k, count=False)))
+    D.close()
+    D = make(swe.AUGRIE)
+    ms_sur = timed(D, lambda D, k: D.surrogate_step(m, k, count=False))
+    rates["surrogate_step"] = cells / (1e-3 * ms_sur)
+    used = D.surrogate_step(m, 1)
+    nedges = D.surrogate_edge_count()
+    D.close()
+
+    def interior(D):
+        a = D.download()[0]
+        return a  # whole domain in host order, ghosts included; compared at equal time below
+
+    ends = {}
+    for name, solver in (("fwave", swe.FWAVE), ("hlle", swe.HLLE), ("surrogate", swe.AUGRIE)):
+        D = make(solver)
+        if name == "surrogate":
+            D.surrogate_step(m, err_steps, count=False)
+        else:
+            D.step(err_steps)
+        ends[name] = (D.time()[0], interior(D).astype(np.float64))
+        D.close()
+    # augmented trajectory around each end time
+    D = make(swe.AUGRIE)
+    targets = sorted((t, k) for k, (t, _) in ends.items())
+    errs, prev, t_prev, dt_last = {}, None, D.time()[0], 0.0
+    while targets:
+        t_next = targets[0][0]
+        if dt_last == 0.0 or t_next - t_prev < 3.0 * dt_last:
+            prev = interior(D).astype(np.float64)
+        D.step(1)
+        t_now = D.time()[0]
+        dt_last, t_cur = t_now - t_prev, t_prev
+        t_prev = t_now
+        while targets and t_now >= targets[0][0]:
+            t_x, k = targets.pop(0)
+            cur = interior(D).astype(np.float64)
+            w = (t_x - t_cur) / (t_now - t_cur)
+            ref = (1 - w) * prev + w * cur
+            errs[k] = float(np.abs(ends[k][1] - ref).sum() / cells)
+    D.close()
+    m.close()
+    flop_edge = 2 * (6 * 64 + 2 * 64 * 64 + 64 * 4)
+    return {"workload": "surrogate of the augmented solver, shoreline ramp 4096x4096 as 4x4 blocks of 1024^2, unsplit",
+            "unit": "cell-updates/s", "rates": rates,
+            "speedup_vs_augmented_step": rates["surrogate_step"] / rates["augmented_step"],
+            "surrogate_edge_fraction": used / nedges,
+            "mlp_flop_per_edge": flop_edge,
+            "mlp_tflops_over_step": nedges * flop_edge / (1e-3 * ms_sur) / 1e12,
+            "l1_error_per_cell_vs_augmented": errs, "error_steps": err_steps,
+            "training": {"edges": int(E.shape[1]), "epochs": epochs, "batch": 8192, "seconds": train_s,
+                         "edges_per_s": epochs * E.shape[1] / train_s, "loss_first_epoch": float(losses[0]),
+                         "loss_last_epoch": float(losses[-1])}}
+
+
 def run_gb300(args, world, rank, local):
     import torch
     import swe_gb300 as swe
@@ -391,6 +502,7 @@ def run_gb300(args, world, rank, local):
 
     lts = lts_measure(swe, local)
     ens = ensemble_measure(swe, local)
+    sur = surrogate_measure(swe, local) if rank == 0 else None
     base = cpu_baseline(float(os.environ.get("SWE_CPU_BASELINE_SECONDS", "12"))) if rank == 0 else None
     if rank == 0:
         line = {
@@ -408,7 +520,7 @@ def run_gb300(args, world, rank, local):
             "e2e": {"value": world * cells / e2e_s, "unit": "cell-updates/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "clocks": clk.summary(), "gpu_launches": launches, "device_status": status,
-            "lts": lts, "ensemble": ens,
+            "lts": lts, "ensemble": ens, "surrogate": sur,
         }
         print(json.dumps(line), flush=True)
     D.close()

@@ -39,6 +39,9 @@ typedef struct swe_mlp swe_mlp;
 int swe_mlp_create(unsigned long long seed, swe_mlp **out);
 void swe_mlp_destroy(swe_mlp *m);
 int swe_mlp_get_params(swe_mlp *m, float *params);
+/* SMs of the device and resident CTAs per SM of the inference kernels (each
+ * holds 64 of the SM's 512 TMEM columns). */
+int swe_mlp_launch_shape(swe_mlp *m, int *sms, int *forward_ctas_per_sm);
 /* Sets the FP32 master parameters and clears the optimiser state. */
 int swe_mlp_set_params(swe_mlp *m, const float *params);
 

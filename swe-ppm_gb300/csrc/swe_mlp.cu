@@ -988,6 +988,13 @@ const char *swe_mlp_last_error(void) { return g_mlpError.c_str(); }
 
 int swe_mlp_param_count(void) { return kNParams; }
 
+int swe_mlp_launch_shape(swe_mlp *m, int *sms, int *forward_ctas_per_sm) {
+    if (!m || !sms || !forward_ctas_per_sm) return mlpFail(SWE_GPU_ERR_INVALID, "null argument");
+    *sms = m->sms;
+    *forward_ctas_per_sm = m->fwdBlocksPerSm;
+    return SWE_GPU_OK;
+}
+
 int swe_mlp_create(unsigned long long seed, swe_mlp **out) {
     if (!out) return mlpFail(SWE_GPU_ERR_INVALID, "null output pointer");
     *out = nullptr;
@@ -998,16 +1005,31 @@ int swe_mlp_create(unsigned long long seed, swe_mlp **out) {
     };
     cudaError_t e = cudaGetDevice(&m->device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&m->sms, cudaDevAttrMultiProcessorCount, m->device);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(trainKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTrSmem);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(forwardKernel<FWD_OUTPUTS>, cudaFuncAttributeMaxDynamicSharedMemorySize, kFwdSmem);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(forwardKernel<FWD_SOLVE>, cudaFuncAttributeMaxDynamicSharedMemorySize, kFwdSmem);
-    if (e == cudaSuccess)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m->fwdBlocksPerSm, forwardKernel<FWD_SOLVE>, 128, kFwdSmem);
+    // shared memory: the largest carveout, so several forward CTAs share an SM
+    auto smemAttr = [&](const void *f, int bytes) {
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    };
+    smemAttr((const void *)trainKernel, kTrSmem);
+    smemAttr((const void *)forwardKernel<FWD_OUTPUTS>, kFwdSmem);
+    smemAttr((const void *)forwardKernel<FWD_SOLVE>, kFwdSmem);
+    smemAttr((const void *)surrogateEdgeKernel<true>, kFwdSmem);
+    // resident inference CTAs per SM from their shared-memory footprint (the
+    // CTA's static and dynamic shared memory plus the 1 KB the SM reserves per
+    // CTA) and registers; TMEM: every resident CTA holds kFwdCols of the SM's
+    // 512 columns.  Extra CTAs of a grid only queue.
+    int smemSm = 0, regsSm = 0;
+    cudaFuncAttributes fa{}, ea{};
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&smemSm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, m->device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&regsSm, cudaDevAttrMaxRegistersPerMultiprocessor, m->device);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, forwardKernel<FWD_SOLVE>);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&ea, surrogateEdgeKernel<true>);
     if (e != cudaSuccess) return bail(mlpFail(SWE_GPU_ERR_CUDA, "create: %s", cudaGetErrorString(e)));
-    // TMEM: every resident forward CTA holds kFwdCols of the SM's 512 columns
-    m->fwdBlocksPerSm = std::max(1, std::min(m->fwdBlocksPerSm, int(512 / kFwdCols)));
+    const int staticSmem = int(std::max(fa.sharedSizeBytes, ea.sharedSizeBytes));
+    const int regs = std::max(fa.numRegs, ea.numRegs);
+    const int bySmem = smemSm / (kFwdSmem + staticSmem + 1024);
+    const int byRegs = regs > 0 ? regsSm / (regs * 128) : 8;
+    m->fwdBlocksPerSm = std::max(1, std::min(std::min(bySmem, byRegs), int(512 / kFwdCols)));
     const size_t pb = kNParams * sizeof(float);
     e = cudaMalloc(&m->p, pb);
     if (e == cudaSuccess) e = cudaMalloc(&m->m, pb);

@@ -48,6 +48,7 @@ EXPORTED = [
     "swe_mlp_last_error", "swe_mlp_gemm_check", "swe_mlp_param_count", "swe_mlp_create", "swe_mlp_destroy",
     "swe_mlp_get_params", "swe_mlp_set_params", "swe_mlp_forward", "swe_mlp_solve", "swe_mlp_loss_grad",
     "swe_mlp_train", "swe_gpu_surrogate_step", "swe_gpu_surrogate_edge_count", "swe_gpu_log_edges",
+    "swe_mlp_launch_shape",
     "swe_nc_open", "swe_nc_write_step", "swe_nc_write_step_slabs", "swe_nc_close",
     "swe_host_scenario_geometry", "swe_host_scenario_boundary", "swe_host_init_block", "swe_host_decompose",
 ]
@@ -118,6 +119,7 @@ def lib():
         L.swe_mlp_destroy.argtypes = [vp]
         L.swe_mlp_destroy.restype = None
         L.swe_mlp_get_params.argtypes = [vp, vp]
+        L.swe_mlp_launch_shape.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int)]
         L.swe_mlp_set_params.argtypes = [vp, vp]
         L.swe_mlp_forward.argtypes = [vp, C.c_int, vp, vp]
         L.swe_mlp_solve.argtypes = [vp, C.c_int, vp, vp, vp, vp]
@@ -525,6 +527,12 @@ class Surrogate:
             self.close()
         except Exception:
             pass
+
+    def launch_shape(self):
+        """(SMs, resident inference CTAs per SM)"""
+        a, b = C.c_int(), C.c_int()
+        _mlp_check(lib().swe_mlp_launch_shape(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
 
     @property
     def params(self):
