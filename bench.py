@@ -399,6 +399,33 @@ def surrogate_measure(swe, device, steps=10, err_steps=120):
                          "loss_last_epoch": float(losses[-1])}}
 
 
+def profile_surrogate(n):
+    """small case for captures of the surrogate kernels: the shoreline ramp on
+    one n x n block, a surrogate trained for 3 epochs on every 8th wet edge of
+    an augmented-solver state after 10 steps, then 4 surrogate steps"""
+    import swe_gb300 as swe
+    geo, h, hu, hv, b = swe.init_domain(swe.SCENARIO_SHORELINE, n, n, 1, [SEED, 50000.0])
+
+    def make(solver):
+        D = swe.Domain(geo["nx_cols"], geo["ny_rows"], geo["dx"], geo["dy"], boundary=geo["boundary"], solver=solver)
+        D.upload(h, hu, hv, b)
+        D.exchange_bathymetry()
+        return D
+
+    A = make(swe.AUGRIE)
+    A.step(10)
+    E, T = A.log_edges(stride=8, capacity=1 << 20)
+    A.close()
+    m = swe.Surrogate(seed=1)
+    m.train(E, T, epochs=3, batch=8192, lr=2e-3, seed=1)
+    D = make(swe.AUGRIE)
+    used = D.surrogate_step(m, 4)
+    log("surrogate edge fraction", used / (4 * D.surrogate_edge_count()))
+    D.close()
+    m.close()
+    return 0
+
+
 def run_gb300(args, world, rank, local):
     import torch
     import swe_gb300 as swe
@@ -536,7 +563,11 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cells", type=int, default=N_CELLS_SIDE, help="cells per side (profiling cases only)")
     ap.add_argument("--profile", action="store_true", help="timed steps only (for ncu captures)")
+    ap.add_argument("--profile-surrogate", type=int, default=0, metavar="N",
+                    help="only the surrogate step on an N x N shoreline (for ncu captures)")
     args = ap.parse_args()
+    if args.profile_surrogate:
+        return profile_surrogate(args.profile_surrogate)
     world, rank, local = dist_init()
     if args.impl == "reference":
         rc = run_reference(args, world, rank)
