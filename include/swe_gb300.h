@@ -94,7 +94,11 @@ typedef struct swe_gpu_desc {
     int speed_pass;      /* 0 = bounded speed pass where available (f-wave or HLLE,
                             unsplit step, CTA tiles): exact wave speeds only where
                             the previous update's speed bounds can reach the
-                            maximum; 1 = every edge.  Both give the same dt. */
+                            maximum; the augmented solver (unsplit, CTA tiles,
+                            global time stepping) solves each edge once into edge
+                            buffers and applies them; 1 = a speed pass over every
+                            edge, then the update pass solving every edge again.
+                            All give the same results bit for bit. */
     float lts_max_timestep; /* > 0: local time stepping with synchronisation
                             intervals of this length (the drivers' -l; unsplit
                             step only; advanced with swe_gpu_lts_advance) */

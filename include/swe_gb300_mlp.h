@@ -83,8 +83,9 @@ int swe_gpu_surrogate_edge_count(swe_gpu_domain *d, long long *edges);
 /* Edge-state logger: after setGhostLayer of the current state, every
  * stride-th edge of the step's edge order with both sides at least 0.1 m deep
  * (up to capacity of them, in edge order) with its augmented-solver net
- * updates: edges 6 x capacity, targets 4 x capacity (row stride capacity),
- * *count of them filled -- training data for swe_mlp_train. */
+ * updates: edges (room for 6 x capacity floats) and targets (4 x capacity) are
+ * returned packed as 6 x count and 4 x count rows -- training data for
+ * swe_mlp_train as they stand. */
 int swe_gpu_log_edges(swe_gpu_domain *d, int stride, int capacity, float *edges, float *targets, int *count);
 
 /* Tensor-core self-check, one CTA, host arrays (row-major), operands rounded

@@ -47,16 +47,22 @@ int fail(int code, const char *fmt, ...) {
 // per ghost cell of one block (blockIdx.y); reads touch only interior cells,
 // writes only ghost cells, so blocks never race.
 // ---------------------------------------------------------------------------
-__global__ void ghostKernel(const DomainDev d, int bathymetry) {
+/// mode 0: state ghosts of the groups still stepping; 1: bathymetry ghosts;
+/// 2: the next step's state ghosts of the groups whose update just finished
+/// (ghostsAhead set), as the two-pass update pass pushes them -- the previous
+/// ring stays in the other buffer for downloads
+__global__ void ghostKernel(const DomainDev d, int mode) {
+    const bool bathymetry = mode == 1;
     const BlockDesc B = d.blocks[blockIdx.y];
     const GroupState *G = d.groups + B.group;
-    if (!bathymetry && !(*((volatile const float *)&G->time) < *((volatile const float *)&G->target))) return;
+    if (mode == 0 && !(*((volatile const float *)&G->time) < *((volatile const float *)&G->target))) return;
+    if (mode == 2 && !*((volatile const int *)&G->ghostsAhead)) return;
     const int cur = G->cur;
     const int nx = B.nx, ny = B.ny;
     const size_t P = size_t(B.pitch);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     // the ghost ring of the current buffer now belongs to the current state
-    if (!bathymetry && threadIdx.x == 0) const_cast<GroupState *>(G)->ghostsAhead = 0;
+    if (mode == 0 && threadIdx.x == 0) const_cast<GroupState *>(G)->ghostsAhead = 0;
     float *fields[3];
     int nf;
     if (bathymetry) {
@@ -272,21 +278,49 @@ struct swe_gpu_domain {
     mlp::EdgeTile *dEdgeTiles = nullptr;
     float *edgeBuf = nullptr;             // 8 fields: x-edge then y-edge net updates
     unsigned long long *dUsed = nullptr;  // edges the surrogate solved
+    // augmented solver, unsplit, CTA tiles, global time stepping: the step
+    // solves every edge once into the edge buffers (computeNumericalFluxes)
+    // and applies them (updateUnknowns) instead of solving each edge in both
+    // the speed and the update pass
+    bool edgeBuffered = false;
 };
 
 namespace {
 
-int enqueueGhost(swe_gpu_domain *D, int bathymetry) {
+/// ghost kernel launch; mode as ghostKernel's
+int enqueueGhost(swe_gpu_domain *D, int mode) {
     const int threads = 128;
     dim3 grid((D->maxPerimeter + threads - 1) / threads, unsigned(D->blocks.size()));
-    ghostKernel<<<grid, threads, 0, D->stream>>>(D->dev, bathymetry);
+    ghostKernel<<<grid, threads, 0, D->stream>>>(D->dev, mode);
     CUDA_TRY(cudaGetLastError());
     D->launches++;
     return SWE_GPU_OK;
 }
 
+mlp::EdgeUpdates edgeUpdates(const swe_gpu_domain *D) {
+    mlp::EdgeUpdates u;
+    for (int k = 0; k < 4; k++) {
+        u.x[k] = D->edgeBuf + size_t(k) * D->fieldElems;
+        u.y[k] = D->edgeBuf + size_t(4 + k) * D->fieldElems;
+    }
+    return u;
+}
+
+long long maxBlockCells(const swe_gpu_domain *D) {
+    long long m = 0;
+    for (const BlockDesc &B : D->blocks) m = std::max(m, (long long)B.nx * B.ny);
+    return m;
+}
+
 int enqueueSpeed(swe_gpu_domain *D) {
     DomainDev d = D->dev;
+    if (D->edgeBuffered) {
+        CUDA_TRY(mlp::launchSurrogateEdges(d, nullptr, D->dEdgeTiles, int(D->edgeTiles.size()), edgeUpdates(D), D->dUsed,
+                                           D->stream));
+        CUDA_TRY(mlp::launchSurrogateDt(d, D->ngroups, D->stream));
+        D->launches += 2;
+        return SWE_GPU_OK;
+    }
     if (D->bounded) {
         CUDA_TRY(launchSpeedBound(d, D->gridB, D->stream));
         D->launches++;
@@ -301,6 +335,16 @@ int enqueueSpeed(swe_gpu_domain *D) {
 
 int enqueueUpdate(swe_gpu_domain *D) {
     DomainDev d = D->dev;
+    if (D->edgeBuffered) {
+        CUDA_TRY(mlp::launchSurrogateApply(d, edgeUpdates(D), int(D->blocks.size()), maxBlockCells(D), D->stream));
+        CUDA_TRY(mlp::launchSurrogateFinish(d, D->ngroups, D->stream));
+        D->launches += 2;
+        // the new state's ghost ring, as the two-pass update leaves it
+        int rc = enqueueGhost(D, 2);
+        if (rc) return rc;
+        D->ghostsValid = true;
+        return SWE_GPU_OK;
+    }
     d.units = D->dUnitsU;
     d.ctaSeg = D->dCtaSegU;
     CUDA_TRY(launchUpdate(d, D->gridU, D->tileRows, D->stream));
@@ -623,6 +667,14 @@ int buildDomain(const std::vector<BlockSpec> &spec, const DomainOptions &o, swe_
         for (int f = 0; f < 3 && ok; f++)
             ok = cudaMalloc(&D->dRing[f], sizeof(float) * std::max(1LL, D->ringElems)) == cudaSuccess;
     }
+    D->edgeBuffered = D->solver == SOLVER_AUGRIE && D->semantics == SEM_UNSPLIT && !D->lts && D->variant == VARIANT_TILE &&
+                      o.speedPass == 0;
+    if (D->edgeBuffered) {
+        D->edgeTiles = mlp::buildEdgeTiles(D->blocks);
+        ok = ok && cudaMalloc(&D->edgeBuf, 8 * bytes) == cudaSuccess;
+        ok = ok && cudaMalloc(&D->dUsed, sizeof(unsigned long long)) == cudaSuccess;
+        ok = ok && cudaMalloc(&D->dEdgeTiles, sizeof(mlp::EdgeTile) * std::max<size_t>(1, D->edgeTiles.size())) == cudaSuccess;
+    }
     if (D->bounded) {
         ok = ok && cudaMalloc(&D->dTiles, sizeof(TileInfo) * D->tiles.size()) == cudaSuccess;
         ok = ok && cudaMalloc(&D->dTileW, sizeof(unsigned int) * 2 * D->tiles.size()) == cudaSuccess;
@@ -640,6 +692,9 @@ int buildDomain(const std::vector<BlockSpec> &spec, const DomainOptions &o, swe_
     }
     cudaMemsetAsync(D->b, 0, bytes, D->stream);
     cudaMemcpyAsync(D->dBlocks, D->blocks.data(), sizeof(BlockDesc) * D->blocks.size(), cudaMemcpyHostToDevice, D->stream);
+    if (D->edgeBuffered && !D->edgeTiles.empty())
+        cudaMemcpyAsync(D->dEdgeTiles, D->edgeTiles.data(), sizeof(mlp::EdgeTile) * D->edgeTiles.size(),
+                        cudaMemcpyHostToDevice, D->stream);
     cudaMemcpyAsync(D->dUnits, D->units.data(), sizeof(WorkUnit) * D->units.size(), cudaMemcpyHostToDevice, D->stream);
     cudaMemcpyAsync(D->dCtaSeg, D->ctaSeg.data(), sizeof(int) * D->ctaSeg.size(), cudaMemcpyHostToDevice, D->stream);
     cudaMemcpyAsync(D->dUnitsU, D->unitsU.data(), sizeof(WorkUnit) * D->unitsU.size(), cudaMemcpyHostToDevice, D->stream);
@@ -1495,7 +1550,7 @@ int swe_gpu_surrogate_step(swe_gpu_domain *dom, swe_mlp *m, int nsteps, long lon
     }
     // the ghost ring of the new state, as the regular update pass leaves it
     if (nsteps > 0) {
-        if ((rc = enqueueGhost(dom, 0))) return rc;
+        if ((rc = enqueueGhost(dom, 2))) return rc;
     }
     dom->ghostsValid = true;
     if (surrogate_edges) {
@@ -1546,6 +1601,9 @@ int swe_gpu_log_edges(swe_gpu_domain *dom, int stride, int capacity, float *edge
         for (int f = 0; f < 4; f++) targets[size_t(f) * capacity + c] = hs[size_t(6 + f) * nslots + k];
         c++;
     }
+    // rows of length c (packed in place; row f moves down from f * capacity)
+    for (int f = 1; f < 6; f++) memmove(edges + size_t(f) * c, edges + size_t(f) * capacity, size_t(c) * sizeof(float));
+    for (int f = 1; f < 4; f++) memmove(targets + size_t(f) * c, targets + size_t(f) * capacity, size_t(c) * sizeof(float));
     *count = c;
     return SWE_GPU_OK;
 }

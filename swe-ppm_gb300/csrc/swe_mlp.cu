@@ -683,7 +683,9 @@ __device__ __forceinline__ void flushSpeed(const DomainDev &d, int group, float 
 
 /// edge pass over a contiguous range of tiles per CTA (so the group changes
 /// rarely within a CTA).  SURR: surrogate with the gate, else the augmented
-/// solver on every edge.
+/// solver on every edge (the default step of augmented-solver domains).
+/// Groups whose time reached their target (or that sit the step out) are
+/// skipped, in this and the following kernels of the step.
 template <bool SURR>
 __global__ void __launch_bounds__(128) surrogateEdgeKernel(const DomainDev d, const uint8_t *image, const EdgeTile *tiles,
                                                            int ntiles, EdgeUpdates u, unsigned long long *usedCount,
@@ -721,6 +723,7 @@ __global__ void __launch_bounds__(128) surrogateEdgeKernel(const DomainDev d, co
             if (group >= 0) flushSpeed(d, group, smax, sMax);
             group = B.group;
         }
+        if (!groupActive(d.groups + group)) continue;  // the group reached its target (CTA-uniform)
         const int cur = d.groups[group].cur;
         float q[6] = {1.f, 1.f, 0.f, 0.f, 0.f, 0.f};
         long long oL;
@@ -776,6 +779,7 @@ __global__ void surrogateDtKernel(const DomainDev d, int ngroups) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= ngroups) return;
     GroupState *G = d.groups + g;
+    if (!groupActive(G)) return;
     const float s = __uint_as_float(G->speedBits);
     const BlockDesc &F = d.blocks[G->firstBlock];
     G->speed = s;
@@ -790,7 +794,7 @@ __global__ void surrogateApplyKernel(const DomainDev d, EdgeUpdates u) {
     const BlockDesc B = d.blocks[blockIdx.y];
     GroupState *G = d.groups + B.group;
     const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= (long long)B.nx * B.ny) return;
+    if (idx >= (long long)B.nx * B.ny || !groupActive(G)) return;
     const int i = int(idx / B.ny) + 1, j = int(idx % B.ny) + 1;
     const int cur = G->cur;
     const float dt = G->dt;
@@ -819,10 +823,11 @@ __global__ void surrogateFinishKernel(const DomainDev d, int ngroups) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= ngroups) return;
     GroupState *G = d.groups + g;
+    if (!groupActive(G)) return;
     G->time = G->time + G->dt;
     G->steps = G->steps + 1;
     G->cur = G->cur ^ 1;
-    G->ghostsAhead = 0;  // the new buffer's ghost ring is stale
+    G->ghostsAhead = 1;  // the next ghost kernel (mode 2) fills the new buffer's ring; the old ring stays readable
     G->boundsValid[0] = 0;
     G->boundsValid[1] = 0;
 }

@@ -401,11 +401,12 @@ class Domain:
     def log_edges(self, stride=1, capacity=1 << 20):
         """wet edge states of the current state and their augmented-solver net
         updates: (edges 6 x count, targets 4 x count)"""
-        e = np.zeros((6, capacity), np.float32)
-        t = np.zeros((4, capacity), np.float32)
+        e = np.zeros(6 * capacity, np.float32)
+        t = np.zeros(4 * capacity, np.float32)
         c = C.c_int()
         _check(lib().swe_gpu_log_edges(self.handle, int(stride), int(capacity), _p(e), _p(t), C.byref(c)))
-        return e[:, :c.value].copy(), t[:, :c.value].copy()
+        n = c.value
+        return e[:6 * n].reshape(6, n).copy(), t[:4 * n].reshape(4, n).copy()
 
     def block_steps(self):
         """update steps each block has executed"""

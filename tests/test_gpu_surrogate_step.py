@@ -13,8 +13,9 @@ from helpers import assert_bitwise
 pytestmark = pytest.mark.gpu
 
 
-def make(swe, geo, st, solver):
-    D = swe.Domain(geo["nx_cols"], geo["ny_rows"], geo["dx"], geo["dy"], boundary=geo["boundary"], solver=solver)
+def make(swe, geo, st, solver, speed_pass=0):
+    D = swe.Domain(geo["nx_cols"], geo["ny_rows"], geo["dx"], geo["dy"], boundary=geo["boundary"], solver=solver,
+                   speed_pass=speed_pass)
     D.upload(*st)
     D.exchange_bathymetry()
     return D
@@ -29,18 +30,46 @@ CASES = [
 
 
 @pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
+def test_default_augmented_step_equals_two_pass_step(swe, case):
+    """The default step of an augmented-solver domain (each edge solved once
+    into the edge buffers) against the two-pass step, with advance() and the
+    split API, ghost rings included."""
+    name, sid, nx, ny, nb, params = case
+    geo, h, hu, hv, b = swe.init_domain(sid, nx, ny, nb, params)
+    st = (h, hu, hv, b)
+    outs = []
+    for sp in (1, 0):
+        D = make(swe, geo, st, swe.AUGRIE, speed_pass=sp)
+        D.advance(1e30, max_steps=9)
+        dts = []
+        for _ in range(4):
+            D.set_ghost_layer()
+            D.compute_fluxes()
+            dts.append(D.max_timestep())
+            D.update_unknowns()
+        outs.append((D.download(), D.time(), np.asarray(dts, np.float32)))
+        assert D.status() == 0
+        D.close()
+    (a, ta, da), (b_, tb, db) = outs
+    assert ta[1] == tb[1] == 13 and np.float32(ta[0]) == np.float32(tb[0])
+    assert_bitwise(da, db, "dt")
+    for x, y, k in zip(a, b_, "h hu hv b".split()):
+        assert_bitwise(x, y, k)
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
 def test_augmented_solver_through_edge_buffers_is_bitwise(swe, case):
     name, sid, nx, ny, nb, params = case
     geo, h, hu, hv, b = swe.init_domain(sid, nx, ny, nb, params)
     st = (h, hu, hv, b)
-    A = make(swe, geo, st, swe.AUGRIE)
+    A = make(swe, geo, st, swe.AUGRIE, speed_pass=1)  # two passes, every edge solved in both
     A.step(12)
     ref = A.download()
     tref, nref = A.time()
     A.close()
-    S = make(swe, geo, st, swe.AUGRIE)
+    S = make(swe, geo, st, swe.AUGRIE, speed_pass=1)
     used = S.surrogate_step(None, 7)
-    S.step(5)  # regular steps continue from the surrogate path's state
+    S.step(5)  # two-pass steps continue from the edge-buffer path's state
     out = S.download()
     t, n = S.time()
     assert S.status() == 0
