@@ -143,6 +143,18 @@ int swe_gpu_download_block(swe_gpu_domain *dom, int block, float *h, float *hu, 
  * memory reaches full link bandwidth).  Both return when the copy is done. */
 int swe_gpu_upload_domain(swe_gpu_domain *dom, const float *h, const float *hu, const float *hv, const float *b);
 int swe_gpu_download_domain(swe_gpu_domain *dom, float *h, float *hu, float *hv, float *b);
+/* Asynchronous forms of the two, for pipelines that keep the link busy in both
+ * directions -- no counterpart in the reference (its blocks live in host
+ * memory).  The host arrays should be pinned; they are read / written after
+ * the call returns, in stream order: an upload's inputs must stay unchanged
+ * and a download's outputs unread until swe_gpu_sync.  Uploads and downloads
+ * each go through two staging slots and a stream of their own, so the link
+ * carries step k's results and step k+1's inputs at the same time as the
+ * device computes.  The first call of each allocates its slots (8 floats per
+ * cell): make both before any stream capture. */
+int swe_gpu_upload_domain_async(swe_gpu_domain *dom, const float *h, const float *hu, const float *hv,
+                                const float *b);
+int swe_gpu_download_domain_async(swe_gpu_domain *dom, float *h, float *hu, float *hv, float *b);
 
 /* Checkpoint snapshot of one block without stopping the simulation: a device
  * kernel writes the current interior of h, hu, hv as big-endian (y, x) slabs
@@ -229,6 +241,7 @@ int swe_gpu_launch_count(const swe_gpu_domain *dom, long long *count);
 int swe_gpu_speed_pass_stats(swe_gpu_domain *dom, int *tiles, int *evaluated);
 int swe_gpu_set_time(swe_gpu_domain *dom, float t);
 
+/* waits for everything queued on the domain (steps, transfers, async downloads) */
 int swe_gpu_sync(swe_gpu_domain *dom);
 /* device-side status bits (bit 0: NaN wave speed); 0 when healthy */
 int swe_gpu_status(swe_gpu_domain *dom, int *status);

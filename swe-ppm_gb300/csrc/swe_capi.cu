@@ -283,6 +283,19 @@ struct swe_gpu_domain {
     // and applies them (updateUnknowns) instead of solving each edge in both
     // the speed and the update pass
     bool edgeBuffered = false;
+    // asynchronous downloads: two staging slots (4 fields each), copied out on
+    // a second stream so one step's download overlaps the next one's upload
+    float *stageDown[2] = {nullptr, nullptr};
+    cudaStream_t copyStream = nullptr;
+    cudaEvent_t downReady[2] = {nullptr, nullptr}, downDone[2] = {nullptr, nullptr};
+    int downSlot = 0;
+    bool downUsed[2] = {false, false};
+    // asynchronous uploads: two staging slots filled on a third stream
+    float *stageUp[2] = {nullptr, nullptr};
+    cudaStream_t upStream = nullptr;
+    cudaEvent_t upReady[2] = {nullptr, nullptr}, upConsumed[2] = {nullptr, nullptr};
+    int upSlot = 0;
+    bool upUsed[2] = {false, false};
 };
 
 namespace {
@@ -420,6 +433,24 @@ void freeDomain(swe_gpu_domain *D) {
     cudaFree(D->dEdgeTiles);
     cudaFree(D->edgeBuf);
     cudaFree(D->dUsed);
+    for (int j = 0; j < 2; j++) {
+        cudaFree(D->stageDown[j]);
+        if (D->downReady[j]) cudaEventDestroy(D->downReady[j]);
+        if (D->downDone[j]) cudaEventDestroy(D->downDone[j]);
+    }
+    if (D->copyStream) {
+        cudaStreamSynchronize(D->copyStream);
+        cudaStreamDestroy(D->copyStream);
+    }
+    for (int j = 0; j < 2; j++) {
+        cudaFree(D->stageUp[j]);
+        if (D->upReady[j]) cudaEventDestroy(D->upReady[j]);
+        if (D->upConsumed[j]) cudaEventDestroy(D->upConsumed[j]);
+    }
+    if (D->upStream) {
+        cudaStreamSynchronize(D->upStream);
+        cudaStreamDestroy(D->upStream);
+    }
     if (D->ownStream) cudaStreamDestroy(D->ownStream);
     delete D;
 }
@@ -979,6 +1010,80 @@ int swe_gpu_download_domain(swe_gpu_domain *dom, float *h, float *hu, float *hv,
     return stageTransfer(dom, 0, int(dom->blocks.size()), host, dom->blocks[0].ny + 2, false, true);
 }
 
+int swe_gpu_upload_domain_async(swe_gpu_domain *dom, const float *h, const float *hu, const float *hv,
+                                const float *b) {
+    if (!dom) return fail(SWE_GPU_ERR_INVALID, "null domain handle");
+    CUDA_TRY(cudaSetDevice(dom->device));
+    const float *host[4] = {h, hu, hv, b};
+    int mask = 0;
+    for (int f = 0; f < 4; f++)
+        if (host[f]) mask |= 1 << f;
+    if (!mask) return SWE_GPU_OK;
+    if (!dom->upStream) {
+        CUDA_TRY(cudaStreamCreateWithFlags(&dom->upStream, cudaStreamNonBlocking));
+        for (int j = 0; j < 2; j++) {
+            CUDA_TRY(cudaMalloc(&dom->stageUp[j], sizeof(float) * 4 * size_t(dom->stageElems)));
+            CUDA_TRY(cudaEventCreateWithFlags(&dom->upReady[j], cudaEventDisableTiming));
+            CUDA_TRY(cudaEventCreateWithFlags(&dom->upConsumed[j], cudaEventDisableTiming));
+        }
+    }
+    const int j = dom->upSlot;
+    dom->upSlot ^= 1;
+    // slot j is free once the repack of its previous use has read it
+    if (dom->upUsed[j]) CUDA_TRY(cudaStreamWaitEvent(dom->upStream, dom->upConsumed[j], 0));
+    const size_t n = size_t(dom->stageElems);
+    for (int f = 0; f < 4; f++)
+        if (host[f])
+            CUDA_TRY(cudaMemcpyAsync(dom->stageUp[j] + size_t(f) * n, host[f], n * sizeof(float), cudaMemcpyHostToDevice,
+                                     dom->upStream));
+    CUDA_TRY(cudaEventRecord(dom->upReady[j], dom->upStream));
+    CUDA_TRY(cudaStreamWaitEvent(dom->stream, dom->upReady[j], 0));
+    const dim3 grid(unsigned(dom->maxCols), unsigned(dom->blocks.size()));
+    repackKernel<<<grid, 256, 0, dom->stream>>>(dom->dev, dom->stageUp[j], dom->stageElems, 1, mask, 0);
+    CUDA_TRY(cudaGetLastError());
+    dom->launches++;
+    CUDA_TRY(cudaEventRecord(dom->upConsumed[j], dom->stream));
+    dom->upUsed[j] = true;
+    dom->ghostsValid = false;
+    return SWE_GPU_OK;
+}
+
+int swe_gpu_download_domain_async(swe_gpu_domain *dom, float *h, float *hu, float *hv, float *b) {
+    if (!dom) return fail(SWE_GPU_ERR_INVALID, "null domain handle");
+    CUDA_TRY(cudaSetDevice(dom->device));
+    float *const host[4] = {h, hu, hv, b};
+    int mask = 0;
+    for (int f = 0; f < 4; f++)
+        if (host[f]) mask |= 1 << f;
+    if (!mask) return SWE_GPU_OK;
+    if (!dom->copyStream) {
+        CUDA_TRY(cudaStreamCreateWithFlags(&dom->copyStream, cudaStreamNonBlocking));
+        for (int j = 0; j < 2; j++) {
+            CUDA_TRY(cudaMalloc(&dom->stageDown[j], sizeof(float) * 4 * size_t(dom->stageElems)));
+            CUDA_TRY(cudaEventCreateWithFlags(&dom->downReady[j], cudaEventDisableTiming));
+            CUDA_TRY(cudaEventCreateWithFlags(&dom->downDone[j], cudaEventDisableTiming));
+        }
+    }
+    const int j = dom->downSlot;
+    dom->downSlot ^= 1;
+    // slot j is free once the copies out of its previous use have finished
+    if (dom->downUsed[j]) CUDA_TRY(cudaStreamWaitEvent(dom->stream, dom->downDone[j], 0));
+    const dim3 grid(unsigned(dom->maxCols), unsigned(dom->blocks.size()));
+    repackKernel<<<grid, 256, 0, dom->stream>>>(dom->dev, dom->stageDown[j], dom->stageElems, 0, mask, 0);
+    CUDA_TRY(cudaGetLastError());
+    dom->launches++;
+    CUDA_TRY(cudaEventRecord(dom->downReady[j], dom->stream));
+    CUDA_TRY(cudaStreamWaitEvent(dom->copyStream, dom->downReady[j], 0));
+    const size_t n = size_t(dom->stageElems);
+    for (int f = 0; f < 4; f++)
+        if (host[f])
+            CUDA_TRY(cudaMemcpyAsync(host[f], dom->stageDown[j] + size_t(f) * n, n * sizeof(float),
+                                     cudaMemcpyDeviceToHost, dom->copyStream));
+    CUDA_TRY(cudaEventRecord(dom->downDone[j], dom->copyStream));
+    dom->downUsed[j] = true;
+    return SWE_GPU_OK;
+}
+
 int swe_gpu_snapshot_slabs_async(swe_gpu_domain *dom, int block, void *h, void *hu, void *hv) {
     int rc = checkBlock(dom, block);
     if (rc) return rc;
@@ -1459,6 +1564,8 @@ int swe_gpu_sync(swe_gpu_domain *dom) {
     if (!dom) return fail(SWE_GPU_ERR_INVALID, "null domain handle");
     CUDA_TRY(cudaSetDevice(dom->device));
     CUDA_TRY(cudaStreamSynchronize(dom->stream));
+    if (dom->copyStream) CUDA_TRY(cudaStreamSynchronize(dom->copyStream));
+    if (dom->upStream) CUDA_TRY(cudaStreamSynchronize(dom->upStream));
     return SWE_GPU_OK;
 }
 

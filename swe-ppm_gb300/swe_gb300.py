@@ -48,7 +48,7 @@ EXPORTED = [
     "swe_mlp_last_error", "swe_mlp_gemm_check", "swe_mlp_param_count", "swe_mlp_create", "swe_mlp_destroy",
     "swe_mlp_get_params", "swe_mlp_set_params", "swe_mlp_forward", "swe_mlp_solve", "swe_mlp_loss_grad",
     "swe_mlp_train", "swe_gpu_surrogate_step", "swe_gpu_surrogate_edge_count", "swe_gpu_log_edges",
-    "swe_mlp_launch_shape",
+    "swe_mlp_launch_shape", "swe_gpu_upload_domain_async", "swe_gpu_download_domain_async",
     "swe_nc_open", "swe_nc_write_step", "swe_nc_write_step_slabs", "swe_nc_close",
     "swe_host_scenario_geometry", "swe_host_scenario_boundary", "swe_host_init_block", "swe_host_decompose",
 ]
@@ -100,6 +100,8 @@ def lib():
         L.swe_gpu_download_block.argtypes = [vp, C.c_int, vp, vp, vp, vp, C.c_int]
         L.swe_gpu_upload_domain.argtypes = [vp, vp, vp, vp, vp]
         L.swe_gpu_download_domain.argtypes = [vp, vp, vp, vp, vp]
+        L.swe_gpu_upload_domain_async.argtypes = [vp, vp, vp, vp, vp]
+        L.swe_gpu_download_domain_async.argtypes = [vp, vp, vp, vp, vp]
         for n in ("swe_gpu_exchange_bathymetry", "swe_gpu_set_ghost_layer", "swe_gpu_compute_fluxes", "swe_gpu_sync"):
             getattr(L, n).argtypes = [vp]
         L.swe_gpu_update_unknowns.argtypes = [vp, C.c_float]
@@ -311,6 +313,24 @@ class Domain:
             if a is not None and (a.dtype != np.float32 or a.size != self.ncells or not a.flags.c_contiguous):
                 raise SweGpuError("download_into needs contiguous float32 arrays of the domain size")
         _check(lib().swe_gpu_download_domain(self.handle, *[_p(a) for a in arrs]))
+
+    def upload_async(self, h=None, hu=None, hv=None, b=None):
+        """asynchronous whole-domain upload from pinned float32 arrays (left
+        unchanged until sync())"""
+        arrs = [None if a is None else a for a in (h, hu, hv, b)]
+        for a in arrs:
+            if a is not None and (a.dtype != np.float32 or a.size != self.ncells or not a.flags.c_contiguous):
+                raise SweGpuError("upload_async needs contiguous float32 arrays of the domain size")
+        _check(lib().swe_gpu_upload_domain_async(self.handle, *[_p(a) for a in arrs]))
+
+    def download_async(self, arrs):
+        """asynchronous download of h, hu, hv (and b) into pinned float32 arrays,
+        valid after sync(); overlaps the next upload"""
+        arrs = list(arrs) + [None] * (4 - len(arrs))
+        for a in arrs:
+            if a is not None and (a.dtype != np.float32 or a.size != self.ncells or not a.flags.c_contiguous):
+                raise SweGpuError("download_async needs contiguous float32 arrays of the domain size")
+        _check(lib().swe_gpu_download_domain_async(self.handle, *[_p(a) for a in arrs]))
 
     def exchange_bathymetry(self):
         _check(lib().swe_gpu_exchange_bathymetry(self.handle))
