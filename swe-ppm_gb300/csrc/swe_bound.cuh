@@ -195,6 +195,7 @@ template <int S> __global__ void __launch_bounds__(256, 4) speedBoundKernel(cons
     __shared__ int sCand[8], sNCand;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int nwb = int(blockDim.x >> 5);
+    pdlWaitAndRelease();
     int grp = -1, cnt = 0;
     unsigned long long bkey = 0ull;  // lane 0: the warp's fastest edge so far (group grp)
     for (long long round = 0;; round++) {

@@ -60,6 +60,15 @@ __device__ __forceinline__ float timestepFromSpeed(float s, float dx, float dy, 
     return FLT_MAX;
 }
 
+/// programmatic dependent launch: wait until the grids this one depends on
+/// have finished and their writes are visible, then let the stream's next
+/// kernel start launching (it waits the same way).  No-ops for a kernel
+/// launched without the programmatic-serialization attribute.
+__device__ __forceinline__ void pdlWaitAndRelease() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 /// buffer p of a double-buffered field without dynamic indexing of the kernel parameter
 __device__ __forceinline__ float *pick(float *const (&f)[2], int p) { return p ? f[1] : f[0]; }
 
@@ -308,6 +317,7 @@ __global__ void __launch_bounds__(kMaxTileRows, 4) sweepKernel(const DomainDev d
     __shared__ float sRed[kMaxTileRows / 32];
     __shared__ int sLast;
     const bool bounds = BOUNDS && d.tileW != nullptr;
+    pdlWaitAndRelease();
 
     const int t = threadIdx.x, TY = blockDim.x;
     const int segEnd = d.ctaSeg[blockIdx.x + 1];
