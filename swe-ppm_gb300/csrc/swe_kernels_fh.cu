@@ -5,23 +5,6 @@
 
 namespace swegb {
 
-/// launch with programmatic stream serialization: the kernel may start while
-/// the previous kernel of the stream finishes; it waits for it on the device
-/// (pdlWaitAndRelease) before touching its results
-template <class... P, class... A>
-static cudaError_t launchPdl(void (*k)(P...), int grid, int block, cudaStream_t s, A... args) {
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(unsigned(grid));
-    cfg.blockDim = dim3(unsigned(block));
-    cfg.dynamicSmemBytes = 0;
-    cfg.stream = s;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    at[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, k, args...);
-}
 
 template <int S> static cudaError_t speed(const DomainDev &d, int n, int th, cudaStream_t s) {
     if (d.variant == VARIANT_WARP) {
@@ -65,7 +48,7 @@ template <int S> static cudaError_t update(const DomainDev &d, int n, int th, cu
     } else if (d.semantics == SEM_SPLIT) {
         sweepKernel<S, SEM_SPLIT, true><<<n, th, 0, s>>>(d);
     } else {
-        cudaError_t e = launchPdl(sweepKernel<S, SEM_UNSPLIT, true>, n, th, s, d);
+        cudaError_t e = launchPdl(sweepKernel<S, SEM_UNSPLIT, true>, dim3(n), dim3(th), s, d);
         if (e != cudaSuccess) return e;
     }
     return cudaGetLastError();
@@ -79,8 +62,8 @@ cudaError_t launchUpdateFH(const DomainDev &d, int n, int th, cudaStream_t s) {
 }
 
 cudaError_t launchSpeedBound(const DomainDev &d, int grid, cudaStream_t s) {
-    cudaError_t e = d.solver == SOLVER_FWAVE ? launchPdl(speedBoundKernel<SOLVER_FWAVE>, grid, 256, s, d)
-                                             : launchPdl(speedBoundKernel<SOLVER_HLLE>, grid, 256, s, d);
+    cudaError_t e = d.solver == SOLVER_FWAVE ? launchPdl(speedBoundKernel<SOLVER_FWAVE>, dim3(grid), dim3(256), s, d)
+                                             : launchPdl(speedBoundKernel<SOLVER_HLLE>, dim3(grid), dim3(256), s, d);
     if (e != cudaSuccess) return e;
     return cudaGetLastError();
 }

@@ -8,6 +8,24 @@
 
 namespace swegb {
 
+/// launch with programmatic stream serialization: the kernel may start while
+/// the previous kernel of the stream finishes; it waits for it on the device
+/// (pdlWaitAndRelease, swe_sweep.cuh) before touching its results
+template <class... P, class... A>
+inline cudaError_t launchPdl(void (*k)(P...), dim3 grid, dim3 block, cudaStream_t s, A... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k, args...);
+}
+
 // speed pass (computeNumericalFluxes' wave speeds + maxTimestep) and fused
 // solve-and-update pass (updateUnknowns) of the f-wave and HLLE solvers
 cudaError_t launchSpeedFH(const DomainDev &d, int nunits, int threads, cudaStream_t s);

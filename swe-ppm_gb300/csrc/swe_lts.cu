@@ -78,6 +78,7 @@ __device__ __forceinline__ bool perimeterIndex(const BlockDesc &B, int i, int &s
 /// (src/blocks/SWE_DimensionalSplittingMPIOverdecomp.cpp:273-304 with
 /// local time stepping): grid (perimeter chunks, blocks)
 __global__ void ltsExchangeKernel(const DomainDev d) {
+    pdlWaitAndRelease();
     const LtsControl C = *d.ltsCtl;
     if (!ltsRunning(C)) return;
     const int k = blockIdx.y;
@@ -128,6 +129,7 @@ __global__ void ltsExchangeKernel(const DomainDev d) {
 __global__ void ltsCheckKernel(const DomainDev d) {
     __shared__ int sAction[4];  // 0 none, 1 copy, 2 interpolate
     __shared__ float sFactor;
+    pdlWaitAndRelease();
     const int k = blockIdx.x;
     GroupState *G = d.groups + k;
     const LtsControl C = *d.ltsCtl;
@@ -197,6 +199,7 @@ __global__ void ltsCheckKernel(const DomainDev d) {
 /// (hasMaxLocalTimestep, src/blocks/SWE_Block.hh:311-367) the interval is
 /// done: t += Tsync, counters reset (src/examples/swe_mpi_overdecomp.cpp:332-342)
 __global__ void ltsDoneKernel(const DomainDev d) {
+    pdlWaitAndRelease();
     LtsControl &C = *d.ltsCtl;
     if (!ltsRunning(C)) return;
     bool done = true;
@@ -229,16 +232,14 @@ __global__ void ltsDoneKernel(const DomainDev d) {
 
 cudaError_t launchLtsExchange(const DomainDev &d, int maxPerimeter, cudaStream_t s) {
     const int threads = 128;
-    ltsExchangeKernel<<<dim3((maxPerimeter + 4 + threads - 1) / threads, unsigned(d.nblocks)), threads, 0, s>>>(d);
-    return cudaGetLastError();
+    return launchPdl(ltsExchangeKernel, dim3((maxPerimeter + 4 + threads - 1) / threads, unsigned(d.nblocks)),
+                     dim3(threads), s, d);
 }
 cudaError_t launchLtsCheck(const DomainDev &d, cudaStream_t s) {
-    ltsCheckKernel<<<unsigned(d.nblocks), 256, 0, s>>>(d);
-    return cudaGetLastError();
+    return launchPdl(ltsCheckKernel, dim3(unsigned(d.nblocks)), dim3(256), s, d);
 }
 cudaError_t launchLtsDone(const DomainDev &d, cudaStream_t s) {
-    ltsDoneKernel<<<1, 256, 0, s>>>(d);
-    return cudaGetLastError();
+    return launchPdl(ltsDoneKernel, dim3(1), dim3(256), s, d);
 }
 
 } // namespace swegb
