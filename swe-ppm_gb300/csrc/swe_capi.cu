@@ -271,6 +271,7 @@ struct swe_gpu_domain {
     LtsControl *dLtsCtl = nullptr;
     float *dRing[3] = {nullptr, nullptr, nullptr};
     long long ringElems = 0;
+    float *dGhostW = nullptr;  // per block side ghost bounds (local time stepping + bounded speed pass)
     cudaGraphExec_t ltsGraph = nullptr;
     long long ltsGraphKernels = 0;
     // surrogate step and edge logger: edge tiles and the stored net updates
@@ -413,6 +414,7 @@ void freeDomain(swe_gpu_domain *D) {
     cudaFree(D->dLts);
     cudaFree(D->dLtsCtl);
     for (int f = 0; f < 3; f++) cudaFree(D->dRing[f]);
+    cudaFree(D->dGhostW);
     if (D->snapEvent) cudaEventDestroy(D->snapEvent);
     for (int i = 0; i < 2; i++) {
         cudaFree(D->h[i]);
@@ -632,8 +634,9 @@ int buildDomain(const std::vector<BlockSpec> &spec, const DomainOptions &o, swe_
         auto tilesX = [&](int k) { return (D->blocks[k].nx + kBoundTile - 1) / kBoundTile; };
         auto ghostSide = [&](const BlockDesc &B, int side, int nbTile) {
             const int type = B.bnd[side];
-            // local time stepping time-interpolates these ghosts: no bound
-            if (type == CONNECT_WITHIN_RANK) return D->lts ? kNbrUnbounded : nbTile;
+            // local time stepping copies or time-interpolates these ghosts:
+            // the check kernel bounds them side by side
+            if (type == CONNECT_WITHIN_RANK) return D->lts ? kNbrGhostLeft - side : nbTile;
             return (type == OUTFLOW || type == WALL) ? kNbrSelf : kNbrUnbounded;
         };
         for (int k = 0; k < int(D->blocks.size()); k++) {
@@ -706,6 +709,8 @@ int buildDomain(const std::vector<BlockSpec> &spec, const DomainOptions &o, swe_
         ok = ok && cudaMalloc(&D->dUsed, sizeof(unsigned long long)) == cudaSuccess;
         ok = ok && cudaMalloc(&D->dEdgeTiles, sizeof(mlp::EdgeTile) * std::max<size_t>(1, D->edgeTiles.size())) == cudaSuccess;
     }
+    if (D->bounded && D->lts)
+        ok = ok && cudaMalloc(&D->dGhostW, sizeof(float) * 4 * D->blocks.size()) == cudaSuccess;
     if (D->bounded) {
         ok = ok && cudaMalloc(&D->dTiles, sizeof(TileInfo) * D->tiles.size()) == cudaSuccess;
         ok = ok && cudaMalloc(&D->dTileW, sizeof(unsigned int) * 2 * D->tiles.size()) == cudaSuccess;
@@ -776,6 +781,12 @@ int buildDomain(const std::vector<BlockSpec> &spec, const DomainOptions &o, swe_
     D->dev.tileRows = D->tileRows;
     D->dev.lts = D->dLts;
     D->dev.ltsCtl = D->dLtsCtl;
+    D->dev.ghostW = D->dGhostW;
+    if (D->dGhostW) {  // unbounded until the first check kernel fills them
+        std::vector<float> inf(4 * D->blocks.size(), INFINITY);
+        cudaMemcpyAsync(D->dGhostW, inf.data(), sizeof(float) * inf.size(), cudaMemcpyHostToDevice, D->stream);
+        cudaStreamSynchronize(D->stream);
+    }
     for (int f = 0; f < 3; f++) D->dev.ring[f] = D->dRing[f];
     D->dev.tileW = D->dTileW;
     D->dev.tileKey = D->dTileKey;
@@ -1631,6 +1642,8 @@ int swe_gpu_surrogate_step(swe_gpu_domain *dom, swe_mlp *m, int nsteps, long lon
     if (!dom || nsteps < 0) return fail(SWE_GPU_ERR_INVALID, "bad argument");
     if (dom->lts) return fail(SWE_GPU_ERR_INVALID, "local-time-stepping domain: the surrogate step is global");
     if (dom->semantics != SEM_UNSPLIT) return fail(SWE_GPU_ERR_INVALID, "the surrogate step is the unsplit step (semantics 0)");
+    if (m && mlp::deviceOf(m) != dom->device)
+        return fail(SWE_GPU_ERR_INVALID, "surrogate on device %d, domain on device %d", mlp::deviceOf(m), dom->device);
     CUDA_TRY(cudaSetDevice(dom->device));
     int rc = ensureEdgeTiles(dom);
     if (rc) return rc;

@@ -1273,6 +1273,7 @@ cudaError_t launchLogEdges(const DomainDev &d, const EdgeTile *tiles, int ntiles
 }
 
 int checkDeviceError(swe_mlp *m, const char *what) { return m ? m->checkErr(what) : SWE_GPU_OK; }
+int deviceOf(const swe_mlp *m) { return m ? m->device : -1; }
 
 } // namespace mlp
 } // namespace swegb

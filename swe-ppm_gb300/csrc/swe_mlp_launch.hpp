@@ -62,6 +62,8 @@ cudaError_t launchLogEdges(const DomainDev &d, const EdgeTile *tiles, int ntiles
 /// SWE_GPU_ERR_DEVICE (message set) when a tensor-core wait of the surrogate
 /// ran out of its iteration limit since the last check; waits for the device
 int checkDeviceError(swe_mlp *m, const char *what);
+/// the CUDA device the surrogate's state lives on
+int deviceOf(const swe_mlp *m);
 
 } // namespace mlp
 } // namespace swegb
