@@ -241,11 +241,6 @@ template <int S> __global__ void __launch_bounds__(256, 4) speedBoundKernel(cons
                     } else if (n == kNbrUnbounded) {
                         w0 = INFINITY;
                         w1 = INFINITY;
-                    } else if (n <= kNbrGhostLeft) {
-                        // local time stepping: one group per block
-                        const float g = __ldg(&d.ghostW[4 * I.group + (kNbrGhostLeft - n)]);
-                        w0 = vmax(w0, g);
-                        w1 = vmax(w1, g);
                     }
                 }
                 k0 = __ldg(&d.tileKey[it]);

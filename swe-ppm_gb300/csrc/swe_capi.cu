@@ -271,7 +271,6 @@ struct swe_gpu_domain {
     LtsControl *dLtsCtl = nullptr;
     float *dRing[3] = {nullptr, nullptr, nullptr};
     long long ringElems = 0;
-    float *dGhostW = nullptr;  // per block side ghost bounds (local time stepping + bounded speed pass)
     cudaGraphExec_t ltsGraph = nullptr;
     long long ltsGraphKernels = 0;
     // surrogate step and edge logger: edge tiles and the stored net updates
@@ -414,7 +413,6 @@ void freeDomain(swe_gpu_domain *D) {
     cudaFree(D->dLts);
     cudaFree(D->dLtsCtl);
     for (int f = 0; f < 3; f++) cudaFree(D->dRing[f]);
-    cudaFree(D->dGhostW);
     if (D->snapEvent) cudaEventDestroy(D->snapEvent);
     for (int i = 0; i < 2; i++) {
         cudaFree(D->h[i]);
@@ -621,8 +619,12 @@ int buildDomain(const std::vector<BlockSpec> &spec, const DomainOptions &o, swe_
     // block by block, column of tiles by column of tiles
     bool smallBlocks = true;
     for (const BlockDesc &B : D->blocks) smallBlocks = smallBlocks && B.nx < 65535 && B.ny < 65535;
+    // (not under local time stepping: with one dt group per block every block's
+    // own maximum needs exact edges, so many tiles are candidates and the full
+    // pass, one streaming read of every edge, is faster)
     D->bounded = D->variant == VARIANT_TILE && D->semantics == SEM_UNSPLIT &&
-                 (D->solver == SOLVER_FWAVE || D->solver == SOLVER_HLLE) && o.speedPass == 0 && smallBlocks;
+                 (D->solver == SOLVER_FWAVE || D->solver == SOLVER_HLLE) && o.speedPass == 0 && smallBlocks &&
+                 !D->lts;
     if (D->bounded) {
         int base = 0;
         for (BlockDesc &B : D->blocks) {
@@ -634,9 +636,8 @@ int buildDomain(const std::vector<BlockSpec> &spec, const DomainOptions &o, swe_
         auto tilesX = [&](int k) { return (D->blocks[k].nx + kBoundTile - 1) / kBoundTile; };
         auto ghostSide = [&](const BlockDesc &B, int side, int nbTile) {
             const int type = B.bnd[side];
-            // local time stepping copies or time-interpolates these ghosts:
-            // the check kernel bounds them side by side
-            if (type == CONNECT_WITHIN_RANK) return D->lts ? kNbrGhostLeft - side : nbTile;
+            // local time stepping time-interpolates these ghosts: no bound
+            if (type == CONNECT_WITHIN_RANK) return D->lts ? kNbrUnbounded : nbTile;
             return (type == OUTFLOW || type == WALL) ? kNbrSelf : kNbrUnbounded;
         };
         for (int k = 0; k < int(D->blocks.size()); k++) {
@@ -709,8 +710,6 @@ int buildDomain(const std::vector<BlockSpec> &spec, const DomainOptions &o, swe_
         ok = ok && cudaMalloc(&D->dUsed, sizeof(unsigned long long)) == cudaSuccess;
         ok = ok && cudaMalloc(&D->dEdgeTiles, sizeof(mlp::EdgeTile) * std::max<size_t>(1, D->edgeTiles.size())) == cudaSuccess;
     }
-    if (D->bounded && D->lts)
-        ok = ok && cudaMalloc(&D->dGhostW, sizeof(float) * 4 * D->blocks.size()) == cudaSuccess;
     if (D->bounded) {
         ok = ok && cudaMalloc(&D->dTiles, sizeof(TileInfo) * D->tiles.size()) == cudaSuccess;
         ok = ok && cudaMalloc(&D->dTileW, sizeof(unsigned int) * 2 * D->tiles.size()) == cudaSuccess;
@@ -781,12 +780,6 @@ int buildDomain(const std::vector<BlockSpec> &spec, const DomainOptions &o, swe_
     D->dev.tileRows = D->tileRows;
     D->dev.lts = D->dLts;
     D->dev.ltsCtl = D->dLtsCtl;
-    D->dev.ghostW = D->dGhostW;
-    if (D->dGhostW) {  // unbounded until the first check kernel fills them
-        std::vector<float> inf(4 * D->blocks.size(), INFINITY);
-        cudaMemcpyAsync(D->dGhostW, inf.data(), sizeof(float) * inf.size(), cudaMemcpyHostToDevice, D->stream);
-        cudaStreamSynchronize(D->stream);
-    }
     for (int f = 0; f < 3; f++) D->dev.ring[f] = D->dRing[f];
     D->dev.tileW = D->dTileW;
     D->dev.tileKey = D->dTileKey;

@@ -139,10 +139,6 @@ struct TileInfo {
 };
 constexpr int kNbrSelf = -1;
 constexpr int kNbrUnbounded = -2;
-/// local time stepping: the ghosts of block side s (LEFT, RIGHT, BOTTOM, TOP)
-/// are covered by that side's ghost bound (DomainDev::ghostW): code
-/// kNbrGhostLeft - s
-constexpr int kNbrGhostLeft = -3;
 constexpr int kBoundTile = 32;
 
 struct DomainDev {
@@ -170,8 +166,6 @@ struct DomainDev {
     LtsBlock *lts;
     LtsControl *ltsCtl;
     float *ring[3];                  // receive rings of h, hu, hv
-    float *ghostW;                   // local time stepping: largest cell speed bound of each
-                                     // block side's ghost cells (4 per block), null without
 };
 
 __device__ __forceinline__ float vmin(float a, float b) { return (b < a) ? b : a; }

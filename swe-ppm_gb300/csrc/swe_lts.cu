@@ -193,37 +193,6 @@ __global__ void ltsCheckKernel(const DomainDev d) {
         G->enabled = ltsInSync(L) ? 1 : 0;
         __threadfence();
     }
-    // the bounded speed pass's cover of the ghost ring as it now stands: the
-    // largest cell speed bound of each side's ghost cells (copied or
-    // time-interpolated layers; a bound of an interpolated state never exceeds
-    // the larger bound of its two ends, but the values themselves are at hand)
-    if (d.ghostW) {
-        __shared__ float sGW[4][8];
-        float w[4] = {0.f, 0.f, 0.f, 0.f};
-        for (int i = threadIdx.x; i < 2 * B.ny + 2 * B.nx; i += blockDim.x) {
-            int side, pos;
-            perimeterIndex(B, i, side, pos);
-            int gx, gy, sx, sy;
-            ghostCell(B, side, pos, gx, gy, sx, sy);
-            const size_t o = size_t(gx) * P + gy;
-            const float b = cellSpeedBound(F[0][o], F[1][o], F[2][o]);
-#pragma unroll
-            for (int s = 0; s < 4; s++)
-                if (s == side) w[s] = vmax(w[s], b);
-        }
-#pragma unroll
-        for (int s = 0; s < 4; s++) {
-            float v = w[s];
-            for (int o = 16; o > 0; o >>= 1) v = vmax(v, __shfl_xor_sync(0xffffffffu, v, o));
-            if ((threadIdx.x & 31) == 0) sGW[s][threadIdx.x >> 5] = v;
-        }
-        __syncthreads();
-        if (threadIdx.x < 4) {
-            float v = 0.f;
-            for (int j = 0; j < int(blockDim.x >> 5); j++) v = vmax(v, sGW[threadIdx.x][j]);
-            d.ghostW[4 * k + threadIdx.x] = v;
-        }
-    }
 }
 
 /// end of an inner iteration: once every block has reached its interval end
