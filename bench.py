@@ -119,13 +119,14 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def setup_domain(swe, device, n=N_CELLS_SIDE):
+def setup_domain(swe, device, n=N_CELLS_SIDE, solver=None):
+    solver = swe.HLLE if solver is None else solver
     geo, h, hu, hv, b = swe.init_domain(swe.SCENARIO_TSUNAMI, n, n, N_BLOCKS, [n, SEED, 100000.0])
     tile_rows = int(os.environ.get("SWE_TILE_ROWS", "0"))
     tile_cols = int(os.environ.get("SWE_TILE_COLS", "0"))
     variant = int(os.environ.get("SWE_KERNEL_VARIANT", "0"))
     speed_pass = int(os.environ.get("SWE_SPEED_PASS", "0"))  # 1: evaluate every edge in the speed pass
-    D = swe.Domain(geo["nx_cols"], geo["ny_rows"], geo["dx"], geo["dy"], boundary=geo["boundary"], solver=swe.HLLE,
+    D = swe.Domain(geo["nx_cols"], geo["ny_rows"], geo["dx"], geo["dy"], boundary=geo["boundary"], solver=solver,
                    tile_rows=tile_rows, tile_cols=tile_cols, device=device, kernel_variant=variant,
                    speed_pass=speed_pass)
     D.upload(h, hu, hv, b)
@@ -433,7 +434,8 @@ def run_gb300(args, world, rank, local):
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     n = args.cells
-    D, geo, host = setup_domain(swe, local, n)
+    solvers = {"hlle": swe.HLLE, "fwave": swe.FWAVE, "augrie": swe.AUGRIE, "hybrid": swe.HYBRID}
+    D, geo, host = setup_domain(swe, local, n, solvers[args.profile_solver] if args.profile else swe.HLLE)
     stream = torch.cuda.Stream(dev)  # a real stream handle: the library launches on it
     assert stream.cuda_stream != 0
     D.set_stream(stream.cuda_stream)
@@ -578,6 +580,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cells", type=int, default=N_CELLS_SIDE, help="cells per side (profiling cases only)")
     ap.add_argument("--profile", action="store_true", help="timed steps only (for ncu captures)")
+    ap.add_argument("--profile-solver", default="hlle", choices=["hlle", "fwave", "augrie", "hybrid"],
+                    help="solver of the --profile run (the bench itself always runs HLLE)")
     ap.add_argument("--profile-surrogate", type=int, default=0, metavar="N",
                     help="only the surrogate step on an N x N shoreline (for ncu captures)")
     args = ap.parse_args()
