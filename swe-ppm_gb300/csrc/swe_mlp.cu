@@ -1240,10 +1240,19 @@ cudaError_t launchSurrogateEdges(const DomainDev &d, const swe_mlp *m, const Edg
         const int grid = std::min(ntiles, m->sms * m->fwdBlocksPerSm);
         surrogateEdgeKernel<true><<<grid, 128, kFwdSmem, s>>>(d, m->image, tiles, ntiles, u, used, m->err);
     } else {
-        int dev = 0, sms = 0;
+        // the augmented solver alone: as many resident CTAs as registers allow
+        // (latency hiding for its long dependency chains), looked up once per device
+        static int perSm[64] = {0}, smCount[64] = {0};
+        int dev = 0;
         cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        const int grid = std::min(ntiles, sms * 8);
+        if (dev < 0 || dev >= 64) dev = 0;
+        if (!perSm[dev]) {
+            cudaDeviceGetAttribute(&smCount[dev], cudaDevAttrMultiProcessorCount, dev);
+            int occ = 0;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, surrogateEdgeKernel<false>, 128, 0);
+            perSm[dev] = std::max(1, occ);
+        }
+        const int grid = std::min(ntiles, smCount[dev] * perSm[dev]);
         surrogateEdgeKernel<false><<<grid, 128, 0, s>>>(d, nullptr, tiles, ntiles, u, used, nullptr);
     }
     return cudaGetLastError();
