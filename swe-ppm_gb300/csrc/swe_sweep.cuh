@@ -338,6 +338,10 @@ __global__ void __launch_bounds__(kMaxTileRows, 4) sweepKernel(const DomainDev d
         const int yTop = min(y0 + TY - 1, B.ny);
         const bool active = y <= yTop;
         float smax = 0.f;
+        float *__restrict__ HO = pick(d.h, cur ^ 1) + B.base;
+        float *__restrict__ HUO = pick(d.hu, cur ^ 1) + B.base;
+        float *__restrict__ HVO = pick(d.hv, cur ^ 1) + B.base;
+        const bool rimRow = y == 1 || y == B.ny;
 
         float dtdx = 0.f, dtdy = 0.f;
         if (UPDATE) {
@@ -372,7 +376,7 @@ __global__ void __launch_bounds__(kMaxTileRows, 4) sweepKernel(const DomainDev d
 
         float nh = 0.f, nhu = 0.f, nhv = 0.f, nb = 0.f;
         if (active) {
-            const size_t o = size_t(x0 - 1) * P + y;
+            const unsigned o = unsigned(x0 - 1) * unsigned(P) + unsigned(y);
             nh = H[o]; nhu = HU[o]; nhv = HV[o]; nb = BT[o];
         }
         Cell prevX = makeCell(0.f, 0.f, 0.f, 0.f, 0.f, 0.f);
@@ -386,7 +390,7 @@ __global__ void __launch_bounds__(kMaxTileRows, 4) sweepKernel(const DomainDev d
         for (int x = x0 - 1; x <= x1; ++x) {
             const float ch = nh, chu = nhu, chv = nhv, cb = nb;
             if (x < x1 && active) {
-                const size_t o = size_t(x + 1) * P + y;
+                const unsigned o = unsigned(x + 1) * unsigned(P) + unsigned(y);
                 nh = H[o]; nhu = HU[o]; nhv = HV[o]; nb = BT[o];
             }
             Cell cx, cy;
@@ -424,7 +428,14 @@ __global__ void __launch_bounds__(kMaxTileRows, 4) sweepKernel(const DomainDev d
                                 xarg = x - 1;
                             }
                         }
-                        storeCell(d, B, cur ^ 1, P, x - 1, y, hn, hun, hvn);
+                        {
+                            // per-block offsets fit in 32 bits
+                            const unsigned o = unsigned(x - 1) * unsigned(P) + unsigned(y);
+                            HO[o] = hn;
+                            HUO[o] = hun;
+                            HVO[o] = hvn;
+                            if (x - 1 == 1 || x - 1 == B.nx || rimRow) pushGhosts(d, B, cur ^ 1, P, x - 1, y, hn, hun, hvn);
+                        }
                     }
                     pendH = aR;
                     pendHU = auR;
