@@ -289,6 +289,40 @@ def ensemble_measure(swe, device, steps=100, count=256):
             "cells": int(cells.sum()), "ms": ms, "tile_rows": rows, "tile_cols": cols}
 
 
+def split_measure(swe, device, steps=20):
+    """The split step (SWE_DimensionalSplitting: x-sweep over the ghost rows,
+    dt from the x-sweep's speeds, y-sweep with dt/dx) on the same tsunami
+    2048^2 as one block (the reference's split block is a single block), HLLE,
+    maximum reduction of dt.  CUDA events around `steps` steps after warm-up,
+    L2 flushed between steps."""
+    import torch
+    n = N_CELLS_SIDE
+    geo, h, hu, hv, b = swe.init_domain(swe.SCENARIO_TSUNAMI, n, n, 1, [n, SEED, 100000.0])
+    D = swe.Domain(geo["nx_cols"], geo["ny_rows"], geo["dx"], geo["dy"], boundary=geo["boundary"], solver=swe.HLLE,
+                   semantics=swe.SPLIT, device=device)
+    stream = torch.cuda.Stream()
+    D.set_stream(stream.cuda_stream)
+    D.upload(h, hu, hv, b)
+    D.exchange_bathymetry()
+    flush = torch.empty(64 << 20, dtype=torch.float32, device="cuda")
+    with torch.cuda.stream(stream):
+        for _ in range(5):
+            flush.zero_()
+            D.step(1)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        for e0, e1 in ev:
+            flush.zero_()
+            e0.record(stream)
+            D.step(1)
+            e1.record(stream)
+    stream.synchronize()
+    ms = sum(e0.elapsed_time(e1) for e0, e1 in ev) / steps
+    status = D.status()
+    D.close()
+    return {"workload": "split step (SWE_DimensionalSplitting), tsunami 2048x2048 as one block, HLLE",
+            "value": n * n / (ms * 1e-3), "unit": "cell-updates/s", "ms_per_step": ms, "device_status": status}
+
+
 def surrogate_measure(swe, device, steps=10, err_steps=120):
     """MLP surrogate of the augmented Riemann solver at 4096^2: the shoreline
     ramp (bathymetry -4000 m to +50 m across 50 km, seeded Gaussian bump) as
@@ -546,6 +580,7 @@ def run_gb300(args, world, rank, local):
     lts = lts_measure(swe, local)
     ens = ensemble_measure(swe, local)
     sur = surrogate_measure(swe, local) if rank == 0 else None
+    split = split_measure(swe, local) if rank == 0 else None
     base = cpu_baseline(float(os.environ.get("SWE_CPU_BASELINE_SECONDS", "12"))) if rank == 0 else None
     if rank == 0:
         line = {
@@ -564,7 +599,7 @@ def run_gb300(args, world, rank, local):
                     "d2h_bytes_per_step": d2h, "calls": "upload_async, step, download_async; sync at the end",
                     "synchronous_value": world * cells / e2e_sync_s},
             "clocks": clk.summary(), "gpu_launches": launches, "device_status": status,
-            "lts": lts, "ensemble": ens, "surrogate": sur,
+            "lts": lts, "ensemble": ens, "surrogate": sur, "split": split,
         }
         print(json.dumps(line), flush=True)
     D.close()
