@@ -72,7 +72,8 @@ int swe_mlp_train(swe_mlp *m, int n, const float *edges, const float *targets, i
  * unsplit cell update (:458-492); the call ends with setGhostLayer of the
  * new state, as a regular step leaves it.  m == NULL runs the augmented solver on every
  * edge through the same kernels: bit-identical to steps of a domain created
- * with SWE_SOLVER_AUGRIE.  Steps do not stop at an advance target.
+ * with SWE_SOLVER_AUGRIE.  Like a regular step, groups whose time has reached
+ * their advance target (swe_gpu_advance) sit the step out.
  * *surrogate_edges (may be NULL; the call then waits) counts the edges the
  * surrogate solved over the call.  Allocates the edge buffers (8 floats per
  * cell) on first use. */
