@@ -195,6 +195,13 @@ template <int S> __global__ void __launch_bounds__(256, 4) speedBoundKernel(cons
     __shared__ int sCand[8], sNCand;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int nwb = int(blockDim.x >> 5);
+    {
+        // tile records are written only when the domain is built: bring the
+        // first round's into L1 before waiting for the previous kernel
+        const long long slot = (long long)blockIdx.x + (long long)gridDim.x * wib;
+        if (lane == 0 && slot < d.ntiles)
+            prefetchL1(&d.tileInfo[(unsigned long long)slot * d.tileHashMul % (unsigned long long)d.ntiles]);
+    }
     pdlWaitAndRelease();
     int grp = -1, cnt = 0;
     unsigned long long bkey = 0ull;  // lane 0: the warp's fastest edge so far (group grp)

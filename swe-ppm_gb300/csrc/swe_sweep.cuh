@@ -69,6 +69,13 @@ __device__ __forceinline__ void pdlWaitAndRelease() {
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 
+/// pulls the cache lines of an object into L1 ahead of its use
+template <class T> __device__ __forceinline__ void prefetchL1(const T *p) {
+    const char *c = reinterpret_cast<const char *>(p);
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(c));
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(c + sizeof(T) - 1));
+}
+
 /// buffer p of a double-buffered field without dynamic indexing of the kernel parameter
 __device__ __forceinline__ float *pick(float *const (&f)[2], int p) { return p ? f[1] : f[0]; }
 
@@ -317,6 +324,33 @@ __global__ void __launch_bounds__(kMaxTileRows, 4) sweepKernel(const DomainDev d
     __shared__ float sRed[kMaxTileRows / 32];
     __shared__ int sLast;
     const bool bounds = BOUNDS && d.tileW != nullptr;
+    // the partition and the block descriptors are written only when the domain
+    // is built: bring the first segment's into L1 before waiting for the
+    // previous kernel.  The update pass also prefetches the segment's first
+    // columns into L2 from the buffer the group state names now (a hint only:
+    // every value used is loaded after the wait).
+    {
+        const int s0 = d.ctaSeg[blockIdx.x];
+        if (s0 < d.ctaSeg[blockIdx.x + 1]) {
+            const WorkUnit w0 = d.units[s0];
+            const BlockDesc &B0 = d.blocks[w0.block];
+            if (threadIdx.x == 0) prefetchL1(&B0);
+            if (UPDATE) {
+                const int y = w0.y0 + int(threadIdx.x);
+                if (y <= B0.ny + 1) {
+                    // through L2 only: no line of the group state may sit in L1
+                    // when the reads after the wait come
+                    const int c = __ldcg(&d.groups[B0.group].cur);
+                    const size_t P = size_t(B0.pitch);
+                    const float *f[4] = {pick(d.h, c), pick(d.hu, c), pick(d.hv, c), d.b};
+#pragma unroll
+                    for (int k = 0; k < 4; k++)
+                        for (int x = w0.x0 - 1; x <= min(w0.x0 + 2, w0.x1); x++)
+                            asm volatile("prefetch.global.L2 [%0];" ::"l"(f[k] + B0.base + size_t(x) * P + size_t(y)));
+                }
+            }
+        }
+    }
     pdlWaitAndRelease();
 
     const int t = threadIdx.x, TY = blockDim.x;
