@@ -86,12 +86,15 @@ __device__ __forceinline__ unsigned long long umax64(unsigned long long a, unsig
 /// exact speeds of the edges of columns [xa, xb) of a tile: x-edges (x-1|x)
 /// and the y-edges of those columns (the block's top edge in the top rim
 /// tile), plus (nx|nx+1) when xb = nx+1; lane = row y0 + lane, the loads of
-/// all (at most NB) columns issued together.  Returns the lane's fastest edge
-/// as a speed key.
+/// all (at most NB) columns issued together.  An edge is solved only when the
+/// larger speed bound of its two cells (cellSpeedBound, from the cells' own
+/// values, ghosts included) reaches T, a speed some edge of the group has:
+/// every skipped edge is slower than the maximum and cannot attain it.
+/// Returns the lane's fastest edge as a speed key.
 template <int S>
 __device__ __forceinline__ unsigned long long tileColumnsSpeed(const float *H, const float *HU, const float *HV,
                                                                size_t P, const TileInfo &I, long long tile, int xa,
-                                                               int xb, int lane) {
+                                                               int xb, int lane, float T) {
     constexpr int NB = 4;
     const int y = I.y0 + lane;
     const bool active = y < I.y1;
@@ -115,36 +118,47 @@ __device__ __forceinline__ unsigned long long tileColumnsSpeed(const float *H, c
         }
     }
     unsigned long long best = 0ull;
-    Cell prevX, dummy;
-    cellQuantities<S>(h[0], hu[0], hv[0], 0.f, prevX, dummy);
+    float wPrev = cellSpeedBound(h[0], hu[0], hv[0]);
 #pragma unroll
     for (int k = 1; k <= NB + 1; k++) {
         const int x = xa - 1 + k;
         if (x >= xEnd) continue;  // warp-uniform
-        Cell cx, cy, below;
-        cellQuantities<S>(h[k], hu[k], hv[k], 0.f, cx, cy);
-        below.h = __shfl_up_sync(0xffffffffu, cy.h, 1);
-        below.hn = __shfl_up_sync(0xffffffffu, cy.hn, 1);
-        below.u = __shfl_up_sync(0xffffffffu, cy.u, 1);
-        below.sq = __shfl_up_sync(0xffffffffu, cy.sq, 1);
-        below.c = __shfl_up_sync(0xffffffffu, cy.c, 1);
-        below.b = 0.f;
+        const float w = cellSpeedBound(h[k], hu[k], hv[k]);
+        // the cell below: the previous lane's, the tile's lower neighbour for lane 0
+        float hBl = __shfl_up_sync(0xffffffffu, h[k], 1);
+        float hvBl = __shfl_up_sync(0xffffffffu, hv[k], 1);
+        float wBl = __shfl_up_sync(0xffffffffu, w, 1);
         if (active) {
-            const float sx = edgeSpeed<S>(prevX, cx);  // x-edge (x-1 | x)
-            if (sx > 0.f) best = umax64(best, speedKey(sx, edgeCode(tile, I, x, y, 0)));
-            if (k <= NB && x < xb) {                   // a column of the tile: its y-edges
-                if (lane == 0) cellQuantities<S>(hB[k - 1], 0.f, hvB[k - 1], 0.f, dummy, below);
-                const float sy = edgeSpeed<S>(below, cy);
-                if (sy > 0.f) best = umax64(best, speedKey(sy, edgeCode(tile, I, x, y, 1)));
-                if (top) {
-                    Cell above;
-                    cellQuantities<S>(hT[k - 1], 0.f, hvT[k - 1], 0.f, dummy, above);
-                    const float st = edgeSpeed<S>(cy, above);
+            if (!(vmax(wPrev, w) * kBoundMargin < T)) {  // x-edge (x-1 | x)
+                Cell L, R, dummy;
+                cellQuantities<S>(h[k - 1], hu[k - 1], hv[k - 1], 0.f, L, dummy);
+                cellQuantities<S>(h[k], hu[k], hv[k], 0.f, R, dummy);
+                const float sx = edgeSpeed<S>(L, R);
+                if (sx > 0.f) best = umax64(best, speedKey(sx, edgeCode(tile, I, x, y, 0)));
+            }
+            if (k <= NB && x < xb) {                     // a column of the tile: its y-edges
+                if (lane == 0) {
+                    hBl = hB[k - 1];
+                    hvBl = hvB[k - 1];
+                    wBl = cellSpeedBound(hBl, 0.f, hvBl);
+                }
+                if (!(vmax(wBl, w) * kBoundMargin < T)) {
+                    Cell L, R, dummy;
+                    cellQuantities<S>(hBl, 0.f, hvBl, 0.f, dummy, L);
+                    cellQuantities<S>(h[k], hu[k], hv[k], 0.f, dummy, R);
+                    const float sy = edgeSpeed<S>(L, R);
+                    if (sy > 0.f) best = umax64(best, speedKey(sy, edgeCode(tile, I, x, y, 1)));
+                }
+                if (top && !(vmax(w, cellSpeedBound(hT[k - 1], 0.f, hvT[k - 1])) * kBoundMargin < T)) {
+                    Cell L, R, dummy;
+                    cellQuantities<S>(h[k], hu[k], hv[k], 0.f, dummy, L);
+                    cellQuantities<S>(hT[k - 1], 0.f, hvT[k - 1], 0.f, dummy, R);
+                    const float st = edgeSpeed<S>(L, R);
                     if (st > 0.f) best = umax64(best, speedKey(st, edgeCode(tile, I, x, y + 1, 1)));
                 }
             }
         }
-        prevX = cx;
+        wPrev = w;
     }
     return best;
 }
@@ -193,6 +207,7 @@ template <int S> __global__ void __launch_bounds__(256, 4) speedBoundKernel(cons
     __shared__ int sGrp[8], sCnt[8], sTileGrp[8];
     __shared__ unsigned long long sKey[8];
     __shared__ int sCand[8], sNCand;
+    __shared__ float sCandT[8];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int nwb = int(blockDim.x >> 5);
     {
@@ -296,7 +311,11 @@ template <int S> __global__ void __launch_bounds__(256, 4) speedBoundKernel(cons
             float T = 0.f;
             for (int v = 0; v < nwb; v++)
                 if (sTileGrp[v] == tgrp) T = vmax(T, sSamp[v]);
-            if (!(W * kBoundMargin < T)) sCand[atomicAdd(&sNCand, 1)] = wib;
+            if (!(W * kBoundMargin < T)) {
+                const int c = atomicAdd(&sNCand, 1);
+                sCand[c] = wib;
+                sCandT[c] = T;
+            }
         }
         __syncthreads();
         // 3. the candidates of this round, all warps on each
@@ -311,7 +330,7 @@ template <int S> __global__ void __launch_bounds__(256, 4) speedBoundKernel(cons
             unsigned long long k = 0ull;
             if (xa < I.x1)
                 k = tileColumnsSpeed<S>(pick(d.h, cur) + I.base, pick(d.hu, cur) + I.base, pick(d.hv, cur) + I.base,
-                                        size_t(I.pitch), I, ct, xa, min(xa + 4, I.x1), lane);
+                                        size_t(I.pitch), I, ct, xa, min(xa + 4, I.x1), lane, sCandT[c]);
             for (int o = 16; o > 0; o >>= 1) k = umax64(k, __shfl_xor_sync(0xffffffffu, k, o));
             if (lane == 0) sKey[wib] = k;
             __syncthreads();
