@@ -168,11 +168,12 @@ __device__ __forceinline__ unsigned long long tileColumnsSpeed(const float *H, c
 /// and remembers where the fastest edge was
 __device__ __forceinline__ void boundTilesDone(const DomainDev &d, GroupState *G, unsigned long long key, int count) {
     if (key) atomicMax(&G->maxEdge, key);
-    __threadfence();
-    const unsigned prev = atomicAdd(&G->arrived, unsigned(count));
+    const unsigned prev = arriveAcqRel(&G->arrived, unsigned(count));
     if (prev + unsigned(count) == unsigned(G->tiles)) {
-        __threadfence();
-        const unsigned long long k = atomicOr(&G->maxEdge, 0ull);
+        // every CTA's key and candidate count, acquired by the arrival; the
+        // state written here is read by the next kernel after this grid ends
+        const unsigned long long k = __ldcg(&G->maxEdge);
+        const int cands = __ldcg(&G->candidates);
         const float s = __uint_as_float(unsigned(k >> 32));  // every evaluated edge is in the key's maximum
         if (k) {
             const unsigned code = unsigned(k);
@@ -188,12 +189,11 @@ __device__ __forceinline__ void boundTilesDone(const DomainDev &d, GroupState *G
         G->speed = s;
         G->dt = groupTimestep(d, G, s, F.dx, F.dy);
         if (!(s == s)) G->status |= 1;
-        G->lastCandidates = atomicAdd(&G->candidates, 0);
+        G->lastCandidates = cands;
         G->candidates = 0;
         G->speedBits = 0u;
         G->maxEdge = 0ull;
         G->arrived = 0u;
-        __threadfence();
     }
 }
 

@@ -69,6 +69,16 @@ __device__ __forceinline__ void pdlWaitAndRelease() {
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 
+/// arrival of `n` units of work on a pass counter, acquire-release at GPU
+/// scope: the writes and atomics this thread issued before (and, through the
+/// barrier before it, its CTA's) are visible to every thread that sees a later
+/// count, so the last arrival sees all of them.  Returns the previous count.
+__device__ __forceinline__ unsigned arriveAcqRel(unsigned *counter, unsigned n) {
+    unsigned old;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(counter), "r"(n) : "memory");
+    return old;
+}
+
 /// pulls the cache lines of an object into L1 ahead of its use
 template <class T> __device__ __forceinline__ void prefetchL1(const T *p) {
     const char *c = reinterpret_cast<const char *>(p);
@@ -145,13 +155,13 @@ __device__ __forceinline__ void segmentDone(const DomainDev &d, GroupState *G, f
     __syncthreads();
     if (threadIdx.x == 0) {
         if (!UPDATE) atomicMax(&G->speedBits, __float_as_uint(m));
-        __threadfence();
-        const unsigned prev = atomicAdd(&G->arrived, 1u);
+        const unsigned prev = arriveAcqRel(&G->arrived, 1u);
         *sLast = (prev == unsigned(UPDATE ? G->unitsUpd : G->units) - 1u);
     }
     __syncthreads();
+    // the group state the last segment writes is read by the next kernel,
+    // which starts after this grid completes (or waits for it): no fence
     if (*sLast && threadIdx.x == 0) {
-        __threadfence();
         if (UPDATE) {
             G->arrived = 0u;
             G->time = G->time + G->dt;
@@ -162,7 +172,7 @@ __device__ __forceinline__ void segmentDone(const DomainDev &d, GroupState *G, f
             G->boundsValid[cur] = 0;
             G->boundsValid[cur ^ 1] = d.tileW ? 1 : 0;
         } else {
-            float s = __uint_as_float(atomicOr(&G->speedBits, 0u));
+            float s = __uint_as_float(__ldcg(&G->speedBits));  // every CTA's maximum (acquired above)
             const BlockDesc &F = d.blocks[G->firstBlock];
             if (d.semantics == SEM_SPLIT && d.splitDtMode == SPLIT_DT_LAST_EDGE) {
                 // speed of the last x-edge the serial loop solves: (nx | nx+1) in row ny+1
@@ -200,7 +210,6 @@ __device__ __forceinline__ void segmentDone(const DomainDev &d, GroupState *G, f
             G->speedBits = 0u;
             G->arrived = 0u;
         }
-        __threadfence();
     }
 }
 
