@@ -190,8 +190,7 @@ __global__ void ltsCheckKernel(const DomainDev d) {
                 if (L.received[s] != GL_DONE) L.received[s] = (L.received[s] == GL_INTER) ? GL_INTER : GL_NEXT;
         }
         if (ltsInSync(L) && L.stepSizeCounter < L.stepSize) L.stepSizeCounter++;
-        G->enabled = ltsInSync(L) ? 1 : 0;
-        __threadfence();
+        G->enabled = ltsInSync(L) ? 1 : 0;  // read by the next kernels, after this grid ends
     }
 }
 
@@ -224,7 +223,6 @@ __global__ void ltsDoneKernel(const DomainDev d) {
             C.t = C.t + C.maxTimestepLocal;
             C.intervals++;
         }
-        __threadfence();
     }
 }
 

@@ -346,16 +346,26 @@ __global__ void __launch_bounds__(kMaxTileRows, 4) sweepKernel(const DomainDev d
             if (threadIdx.x == 0) prefetchL1(&B0);
             if (UPDATE) {
                 const int y = w0.y0 + int(threadIdx.x);
+                // through L2 only: no line of the group state may sit in L1
+                // when the reads after the wait come
+                const int c = __ldcg(&d.groups[B0.group].cur);
+                const size_t P = size_t(B0.pitch);
+                const float *f[4] = {pick(d.h, c), pick(d.hu, c), pick(d.hv, c), d.b};
                 if (y <= B0.ny + 1) {
-                    // through L2 only: no line of the group state may sit in L1
-                    // when the reads after the wait come
-                    const int c = __ldcg(&d.groups[B0.group].cur);
-                    const size_t P = size_t(B0.pitch);
-                    const float *f[4] = {pick(d.h, c), pick(d.hu, c), pick(d.hv, c), d.b};
 #pragma unroll
                     for (int k = 0; k < 4; k++)
                         for (int x = w0.x0 - 1; x <= min(w0.x0 + 2, w0.x1); x++)
                             asm volatile("prefetch.global.L2 [%0];" ::"l"(f[k] + B0.base + size_t(x) * P + size_t(y)));
+                }
+                // the two cells of this thread's boundary y-edge (see below)
+                const int XC0 = w0.x1 - w0.x0;
+                if (int(threadIdx.x) < 2 * XC0) {
+                    const bool top = int(threadIdx.x) >= XC0;
+                    const int k = top ? int(threadIdx.x) - XC0 : int(threadIdx.x);
+                    const int yl = top ? min(w0.y0 + int(blockDim.x) - 1, B0.ny) : w0.y0 - 1;
+#pragma unroll
+                    for (int q = 0; q < 4; q++)
+                        asm volatile("prefetch.global.L2 [%0];" ::"l"(f[q] + B0.base + size_t(w0.x0 + k) * P + size_t(yl)));
                 }
             }
         }
