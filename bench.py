@@ -570,18 +570,31 @@ def run_gb300(args, world, rank, local):
     algo_bytes = BYTES_PER_CELL * cells
     achieved = algo_bytes / (t_update * 1e-3) / 1e9
     step_achieved = algo_bytes / (ms_per_step * 1e-3) / 1e9
-    traffic = None
+    traffic, warp_inst = None, None
     try:
         with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
-            traffic = json.load(f).get("update_kernel_dram_bytes_per_launch")
+            prof = json.load(f)
+        traffic = prof.get("update_kernel_dram_bytes_per_launch")
+        warp_inst = prof.get("update_kernel_warp_instructions_per_launch")
     except Exception:
         pass
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
 
     lts = lts_measure(swe, local)
     ens = ensemble_measure(swe, local)
     sur = surrogate_measure(swe, local) if rank == 0 else None
     split = split_measure(swe, local) if rank == 0 else None
     base = cpu_baseline(float(os.environ.get("SWE_CPU_BASELINE_SECONDS", "12"))) if rank == 0 else None
+    clocks = clk.summary()
+    issue = None
+    if warp_inst and clocks.get("sm_mhz"):
+        # the update pass is issue-bound: its warp instructions (ncu, one launch)
+        # per second against one instruction per SM sub-partition per cycle
+        issue_peak = sms * 4 * clocks["sm_mhz"] * 1e6
+        issue_achieved = warp_inst / (t_update * 1e-3)
+        issue = {"warp_instructions_per_launch": warp_inst, "achieved": issue_achieved, "peak": issue_peak,
+                 "unit": "warp instructions/s", "frac": issue_achieved / issue_peak,
+                 "peak_from": "%d SMs x 4 sub-partitions x %.0f MHz (median SM clock under load)" % (sms, clocks["sm_mhz"])}
     if rank == 0:
         line = {
             "metric": METRIC, "value": world * cells / (ms_per_step * 1e-3), "unit": "cell-updates/s",
@@ -592,13 +605,13 @@ def run_gb300(args, world, rank, local):
             "roofline": {"bound": "hbm", "kernel": "sweepKernel<HLLE,unsplit,update>", "achieved": achieved,
                          "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "peak_kind": peak_kind,
                          "traffic": traffic, "algorithmic_bytes_per_launch": algo_bytes,
-                         "step_achieved": step_achieved, "step_frac": step_achieved / hbm},
+                         "step_achieved": step_achieved, "step_frac": step_achieved / hbm, "issue": issue},
             "kernel_ms": {"ghost": t_ghost, "speed": t_speed, "update": t_update},
             "cpu_baseline": {k: base[k] for k in ("value", "unit", "cores", "kind", "sample")},
             "e2e": {"value": world * cells / e2e_s, "unit": "cell-updates/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "calls": "upload_async, step, download_async; sync at the end",
                     "synchronous_value": world * cells / e2e_sync_s},
-            "clocks": clk.summary(), "gpu_launches": launches, "device_status": status,
+            "clocks": clocks, "gpu_launches": launches, "device_status": status,
             "lts": lts, "ensemble": ens, "surrogate": sur, "split": split,
         }
         print(json.dumps(line), flush=True)
