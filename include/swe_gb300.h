@@ -176,7 +176,10 @@ int swe_gpu_free_pinned(void *p);
 int swe_gpu_exchange_bathymetry(swe_gpu_domain *dom);
 
 /* setGhostLayer (src/blocks/SWE_DimensionalSplittingMpi.cpp:188-376): boundary
- * conditions and on-device halo copies between blocks */
+ * conditions and on-device halo copies between blocks.  After an update pass
+ * the ring already holds these values (the pass pushed them from the new rim
+ * cells), and the call only marks it as the current state's; after an upload
+ * it recomputes the ring. */
 int swe_gpu_set_ghost_layer(swe_gpu_domain *dom);
 /* computeNumericalFluxes (src/blocks/SWE_DimensionalSplittingMpi.cpp:383-476):
  * wave speeds of every edge and the group's maxTimestep, kept on the device */

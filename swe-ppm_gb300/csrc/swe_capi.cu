@@ -50,12 +50,18 @@ int fail(int code, const char *fmt, ...) {
 /// mode 0: state ghosts of the groups still stepping; 1: bathymetry ghosts;
 /// 2: the next step's state ghosts of the groups whose update just finished
 /// (ghostsAhead set), as the two-pass update pass pushes them -- the previous
-/// ring stays in the other buffer for downloads
+/// ring stays in the other buffer for downloads; 3: the ring is already the
+/// one mode 0 would write (the update pass pushed it): only hand it to the
+/// current state, as mode 0 does
 __global__ void ghostKernel(const DomainDev d, int mode) {
     const bool bathymetry = mode == 1;
     const BlockDesc B = d.blocks[blockIdx.y];
     const GroupState *G = d.groups + B.group;
-    if (mode == 0 && !(*((volatile const float *)&G->time) < *((volatile const float *)&G->target))) return;
+    if ((mode == 0 || mode == 3) && !(*((volatile const float *)&G->time) < *((volatile const float *)&G->target))) return;
+    if (mode == 3) {
+        if (threadIdx.x == 0) const_cast<GroupState *>(G)->ghostsAhead = 0;
+        return;
+    }
     if (mode == 2 && !*((volatile const int *)&G->ghostsAhead)) return;
     const int cur = G->cur;
     const int nx = B.nx, ny = B.ny;
@@ -302,8 +308,8 @@ namespace {
 
 /// ghost kernel launch; mode as ghostKernel's
 int enqueueGhost(swe_gpu_domain *D, int mode) {
-    const int threads = 128;
-    dim3 grid((D->maxPerimeter + threads - 1) / threads, unsigned(D->blocks.size()));
+    const int threads = mode == 3 ? 32 : 128;
+    dim3 grid(mode == 3 ? 1 : (D->maxPerimeter + threads - 1) / threads, unsigned(D->blocks.size()));
     ghostKernel<<<grid, threads, 0, D->stream>>>(D->dev, mode);
     CUDA_TRY(cudaGetLastError());
     D->launches++;
@@ -1139,7 +1145,9 @@ int swe_gpu_set_ghost_layer(swe_gpu_domain *dom) {
     if (dom && dom->lts) return fail(SWE_GPU_ERR_INVALID, "local-time-stepping domain: use swe_gpu_lts_advance");
     if (!dom) return fail(SWE_GPU_ERR_INVALID, "null domain handle");
     CUDA_TRY(cudaSetDevice(dom->device));
-    int rc = enqueueGhost(dom, 0);
+    // after an update pass the ring already holds what setGhostLayer computes
+    // (the pass pushed it from the new rim cells): only mark it current
+    int rc = enqueueGhost(dom, dom->ghostsValid ? 3 : 0);
     if (!rc) dom->ghostsValid = true;
     return rc;
 }

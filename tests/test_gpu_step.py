@@ -111,6 +111,37 @@ def test_random_domains_unsplit(swe, oracle_mod, solver, case, variant):
     compare(gpu, ref, "case %d %s" % (case, solver))
 
 
+@pytest.mark.parametrize("solver", ["hlle", "augrie"])
+@pytest.mark.parametrize("case", [0, 1, 4])
+def test_set_ghost_layer_after_update_equals_recomputed_ring(swe, solver, case):
+    """setGhostLayer right after an update pass only marks the ring the pass
+    pushed as current; the ring must equal the one the ghost kernel computes
+    from scratch for the same interior (walls, outflow, intra-rank copies,
+    corners), bit for bit."""
+    sid, params, nx, ny, nb, outer, tr, tc = CASES[case]
+    geo, h0, hu0, hv0, b0 = swe.init_domain(sid, nx, ny, nb, params, boundary=outer)
+
+    def domain():
+        D = swe.Domain(geo["nx_cols"], geo["ny_rows"], geo["dx"], geo["dy"], boundary=outer, solver=SOLVERS[solver])
+        return D
+
+    D = domain()
+    D.upload(h0, hu0, hv0, b0)
+    D.exchange_bathymetry()
+    D.step(5)
+    D.set_ghost_layer()
+    pushed = D.download()
+    assert D.status() == 0
+    D.close()
+    E = domain()
+    E.upload(*pushed)  # an upload invalidates the ring: the ghost kernel recomputes it
+    E.set_ghost_layer()
+    fresh = E.download()
+    E.close()
+    for a, r, k in zip(pushed, fresh, "h hu hv b".split()):
+        assert_bitwise(a, r, k)
+
+
 @pytest.mark.parametrize("variant", [0, 1, 2, 3])
 @pytest.mark.parametrize("solver", ["hybrid", "hlle", "fwave", "augrie"])
 @pytest.mark.parametrize("mode", [0, 1])
