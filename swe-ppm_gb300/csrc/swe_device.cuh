@@ -304,22 +304,21 @@ __device__ __forceinline__ void waveCurve(float h, float hK, float cK, float &f,
     }
 }
 
-static __device__ __noinline__ void middleState(float hL, float hR, float uL, float uR, float &hm, float &s1m, float &s2m,
-                                         bool &rare1, bool &rare2) {
+/// cL, cR: sqrt(g hL), sqrt(g hR), computed once by the caller
+static __device__ __noinline__ void middleState(float hL, float hR, float uL, float uR, float cL, float cR, float &hm,
+                                                float &s1m, float &s2m, bool &rare1, bool &rare2) {
     if (hR < kDryTol) {
         hm = 0.f;
-        const float front = uL + 2.f * sqrtf(kG * hL);
+        const float front = uL + 2.f * cL;
         s1m = front; s2m = front; rare1 = true; rare2 = false;
         return;
     }
     if (hL < kDryTol) {
         hm = 0.f;
-        const float front = uR - 2.f * sqrtf(kG * hR);
+        const float front = uR - 2.f * cR;
         s1m = front; s2m = front; rare1 = false; rare2 = true;
         return;
     }
-    const float cL = sqrtf(kG * hL);
-    const float cR = sqrtf(kG * hR);
     const float cm = 0.5f * (cL + cR) + 0.25f * (uL - uR);
     if (cm <= 0.f) {
         hm = 0.f;
@@ -374,7 +373,8 @@ static __device__ __noinline__ void edgeAugRie(float hL, float hR, float huL, fl
         uL = huL / hL;
         float hm, s1m, s2m;
         bool r1, r2;
-        middleState(hL, hL, uL, -uL, hm, s1m, s2m, r1, r2);
+        const float c = sqrtf(kG * hL);
+        middleState(hL, hL, uL, -uL, c, c, hm, s1m, s2m, r1, r2);
         const float hTest = vmax(hL, hm);
         if (hTest + bL < bR) {
             wallR = true;
@@ -386,7 +386,8 @@ static __device__ __noinline__ void edgeAugRie(float hL, float hR, float huL, fl
         uR = huR / hR;
         float hm, s1m, s2m;
         bool r1, r2;
-        middleState(hR, hR, -uR, uR, hm, s1m, s2m, r1, r2);
+        const float c = sqrtf(kG * hR);
+        middleState(hR, hR, -uR, uR, c, c, hm, s1m, s2m, r1, r2);
         const float hTest = vmax(hR, hm);
         if (hTest + bR < bL) {
             wallL = true;
@@ -399,12 +400,12 @@ static __device__ __noinline__ void edgeAugRie(float hL, float hR, float huL, fl
         uR = huR / hR;
     }
 
-    float hm, s1m, s2m;
-    bool rare1, rare2;
-    middleState(hL, hR, uL, uR, hm, s1m, s2m, rare1, rare2);
-
     const float cL = sqrtf(kG * hL);
     const float cR = sqrtf(kG * hR);
+    float hm, s1m, s2m;
+    bool rare1, rare2;
+    middleState(hL, hR, uL, uR, cL, cR, hm, s1m, s2m, rare1, rare2);
+
     const float sqL = sqrtf(hL);
     const float sqR = sqrtf(hR);
     const float uRoe = fmaf(uL, sqL, uR * sqR) / (sqL + sqR);
