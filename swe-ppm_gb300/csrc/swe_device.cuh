@@ -305,7 +305,7 @@ __device__ __forceinline__ void waveCurve(float h, float hK, float cK, float &f,
 }
 
 /// cL, cR: sqrt(g hL), sqrt(g hR), computed once by the caller
-static __device__ __noinline__ void middleState(float hL, float hR, float uL, float uR, float cL, float cR, float &hm,
+static __device__ __forceinline__ void middleState(float hL, float hR, float uL, float uR, float cL, float cR, float &hm,
                                                 float &s1m, float &s2m, bool &rare1, bool &rare2) {
     if (hR < kDryTol) {
         hm = 0.f;
@@ -358,7 +358,7 @@ static __device__ __noinline__ void middleState(float hL, float hR, float uL, fl
     s2m = um + cmid;
 }
 
-static __device__ __noinline__ void edgeAugRie(float hL, float hR, float huL, float huR, float bL, float bR, float &hUpdL,
+static __device__ __forceinline__ void edgeAugRie(float hL, float hR, float huL, float huR, float bL, float bR, float &hUpdL,
                                         float &hUpdR, float &huUpdL, float &huUpdR, float &speed) {
     const bool dryL = hL < kDryTol;
     const bool dryR = hR < kDryTol;
