@@ -395,6 +395,28 @@ __global__ void __launch_bounds__(kMaxTileRows, 4) sweepKernel(const DomainDev d
         float *__restrict__ HUO = pick(d.hu, cur ^ 1) + B.base;
         float *__restrict__ HVO = pick(d.hv, cur ^ 1) + B.base;
         const bool rimRow = y == 1 || y == B.ny;
+        // a rim row (y == 1 or y == ny) pushes the ghost below / above each of
+        // its cells every column.  For outflow, wall and intra-rank sides that
+        // is one store per field at rimGhost + x * rimPitch (offsets from the
+        // block's base; a wall negates hv), as pushGhosts does it; every other
+        // case, and the block's first and last columns, go through pushGhosts.
+        int rimMode = 0;  // 0: pushGhosts, 1: copy, 2: copy with -hv
+        long long rimGhost = 0;
+        int rimPitch = 0;
+        if (UPDATE && rimRow && !d.lts && B.ny > 1) {
+            const int side = (y == 1) ? 2 : 3;
+            const int type = B.bnd[side];
+            if (type == OUTFLOW || type == WALL) {
+                rimMode = type == WALL ? 2 : 1;
+                rimGhost = (side == 2) ? 0 : B.ny + 1;
+                rimPitch = B.pitch;
+            } else if (type == CONNECT_WITHIN_RANK) {
+                const BlockDesc &N = d.blocks[B.nbr[side]];
+                rimMode = 1;
+                rimGhost = N.base - B.base + ((side == 2) ? N.ny + 1 : 0);
+                rimPitch = N.pitch;
+            }
+        }
 
         float dtdx = 0.f, dtdy = 0.f;
         if (UPDATE) {
@@ -487,7 +509,16 @@ __global__ void __launch_bounds__(kMaxTileRows, 4) sweepKernel(const DomainDev d
                             HO[o] = hn;
                             HUO[o] = hun;
                             HVO[o] = hvn;
-                            if (x - 1 == 1 || x - 1 == B.nx || rimRow) pushGhosts(d, B, cur ^ 1, P, x - 1, y, hn, hun, hvn);
+                            if (x - 1 == 1 || x - 1 == B.nx || rimRow) {
+                                if (rimMode != 0 && x - 1 != 1 && x - 1 != B.nx) {
+                                    const long long g = rimGhost + (long long)(x - 1) * rimPitch;
+                                    HO[g] = hn;
+                                    HUO[g] = hun;
+                                    HVO[g] = rimMode == 2 ? -hvn : hvn;
+                                } else {
+                                    pushGhosts(d, B, cur ^ 1, P, x - 1, y, hn, hun, hvn);
+                                }
+                            }
                         }
                     }
                     pendH = aR;
