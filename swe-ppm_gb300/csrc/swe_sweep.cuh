@@ -396,25 +396,30 @@ __global__ void __launch_bounds__(kMaxTileRows, 4) sweepKernel(const DomainDev d
         float *__restrict__ HVO = pick(d.hv, cur ^ 1) + B.base;
         const bool rimRow = y == 1 || y == B.ny;
         // a rim row (y == 1 or y == ny) pushes the ghost below / above each of
-        // its cells every column.  For outflow, wall and intra-rank sides that
-        // is one store per field at rimGhost + x * rimPitch (offsets from the
-        // block's base; a wall negates hv), as pushGhosts does it; every other
-        // case, and the block's first and last columns, go through pushGhosts.
-        int rimMode = 0;  // 0: pushGhosts, 1: copy, 2: copy with -hv
+        // its cells every column, as pushGhosts does it: one store per field at
+        // rimGhost + x * rimPitch (offsets from the block's base).  Outflow and
+        // intra-rank sides copy the cell, a wall negates hv, the other types
+        // (and every side under local time stepping) keep the ghost's value
+        // from the input buffer.  The block's first and last columns go
+        // through pushGhosts (corners).  Inline, because the CTA's barrier makes
+        // every warp wait for the rim row's warp each column.
+        int rimMode = 0;  // 0: pushGhosts, 1: copy, 2: copy with -hv, 3: keep
         long long rimGhost = 0;
         int rimPitch = 0;
-        if (UPDATE && rimRow && !d.lts && B.ny > 1) {
+        if (UPDATE && rimRow && B.ny > 1) {
             const int side = (y == 1) ? 2 : 3;
-            const int type = B.bnd[side];
+            const int type = d.lts ? PASSIVE : B.bnd[side];
+            rimGhost = (side == 2) ? 0 : B.ny + 1;
+            rimPitch = B.pitch;
             if (type == OUTFLOW || type == WALL) {
                 rimMode = type == WALL ? 2 : 1;
-                rimGhost = (side == 2) ? 0 : B.ny + 1;
-                rimPitch = B.pitch;
             } else if (type == CONNECT_WITHIN_RANK) {
                 const BlockDesc &N = d.blocks[B.nbr[side]];
                 rimMode = 1;
                 rimGhost = N.base - B.base + ((side == 2) ? N.ny + 1 : 0);
                 rimPitch = N.pitch;
+            } else {
+                rimMode = 3;
             }
         }
 
@@ -512,9 +517,15 @@ __global__ void __launch_bounds__(kMaxTileRows, 4) sweepKernel(const DomainDev d
                             if (x - 1 == 1 || x - 1 == B.nx || rimRow) {
                                 if (rimMode != 0 && x - 1 != 1 && x - 1 != B.nx) {
                                     const long long g = rimGhost + (long long)(x - 1) * rimPitch;
-                                    HO[g] = hn;
-                                    HUO[g] = hun;
-                                    HVO[g] = rimMode == 2 ? -hvn : hvn;
+                                    if (rimMode == 3) {
+                                        HO[g] = H[g];
+                                        HUO[g] = HU[g];
+                                        HVO[g] = HV[g];
+                                    } else {
+                                        HO[g] = hn;
+                                        HUO[g] = hun;
+                                        HVO[g] = rimMode == 2 ? -hvn : hvn;
+                                    }
                                 } else {
                                     pushGhosts(d, B, cur ^ 1, P, x - 1, y, hn, hun, hvn);
                                 }
