@@ -233,7 +233,9 @@ __device__ __forceinline__ void waveSpeeds(const Cell &L, const Cell &R, float &
 
 /// share of a wave with speed s that goes to the left cell: 1, 0 or 1/2
 /// (|s| <= zeroTol); the right cell gets 1 minus that.  Products with these
-/// weights are exact, so weighting equals the branchy routing bit for bit.
+/// weights are exact, and a share of 0 adds a signed zero to a sum that
+/// started at +0 (so never -0), which leaves it unchanged: the weighted sums
+/// (0 + w1 z1) + w2 z2 equal the routing of the two waves in turn, bit for bit.
 __device__ __forceinline__ float leftShare(float s) {
     return (s < -kZeroTol) ? 1.f : ((s > kZeroTol) ? 0.f : 0.5f);
 }
@@ -261,12 +263,20 @@ __device__ __forceinline__ void edgeFH(Cell L, Cell R, float &hUpdL, float &hUpd
     const float rd = 1.f / (s2 - s1);
     const float beta1 = fmaf(s2, df1, -df2) * rd;
     const float beta2 = fmaf(-s1, df1, df2) * rd;
-    const float w1 = leftShare(s1), w2 = leftShare(s2);
     const float z1u = beta1 * s1, z2u = beta2 * s2;
-    hUpdL = fmaf(w2, beta2, w1 * beta1);
-    hUpdR = fmaf(1.f - w2, beta2, (1.f - w1) * beta1);
-    huUpdL = fmaf(w2, z2u, w1 * z1u);
-    huUpdR = fmaf(1.f - w2, z2u, (1.f - w1) * z1u);
+    // the routing of wave 1, then wave 2, into sums that start at +0
+    if (s1 < -kZeroTol && s2 > kZeroTol) {  // subsonic: wave 1 left, wave 2 right
+        hUpdL = 0.f + beta1;
+        huUpdL = 0.f + z1u;
+        hUpdR = 0.f + beta2;
+        huUpdR = 0.f + z2u;
+    } else {
+        const float w1 = leftShare(s1), w2 = leftShare(s2);
+        hUpdL = (0.f + w1 * beta1) + w2 * beta2;
+        hUpdR = (0.f + (1.f - w1) * beta1) + (1.f - w2) * beta2;
+        huUpdL = (0.f + w1 * z1u) + w2 * z2u;
+        huUpdR = (0.f + (1.f - w1) * z1u) + (1.f - w2) * z2u;
+    }
     if (dryL) { hUpdL = 0.f; huUpdL = 0.f; }
     if (dryR) { hUpdR = 0.f; huUpdR = 0.f; }
     speed = fmaxf(fabsf(s1), fabsf(s2));

@@ -34,10 +34,16 @@ def blocks_to_global(arr, nx_cols, ny_rows):
 
 
 def assert_bitwise(a, b, what=""):
+    """Equal bit patterns (so +0 and -0 differ); NaNs match any NaN, whose
+    payload the IEEE operations leave to the implementation."""
     a = np.asarray(a)
     b = np.asarray(b)
     assert a.shape == b.shape, what
-    same = (a == b) | (np.isnan(a) & np.isnan(b))
+    if a.dtype == b.dtype and a.dtype in (np.float32, np.float64):
+        ui = np.uint32 if a.dtype == np.float32 else np.uint64
+        same = (a.view(ui) == b.view(ui)) | (np.isnan(a) & np.isnan(b))
+    else:
+        same = (a == b) | (np.isnan(a) & np.isnan(b))
     if not same.all():
         idx = np.argwhere(~same)[:5]
         raise AssertionError("%s: %d of %d values differ, first %s: %s vs %s" % (

@@ -49,3 +49,23 @@ def test_seeded_edges(swe, oracle_mod, name):
     ref = oracle_mod.solve_edges(SOLVERS[name], *ins)
     for o, r, k in zip(outs, ref, ("hUpdL", "hUpdR", "huUpdL", "huUpdR", "speed")):
         assert_bitwise(o, r, k)
+
+
+def signed_zero_edges():
+    """every combination of dry, near-dry and wet depths with momenta and
+    bathymetry of both zero signs, tiny and moderate values: lakes at rest,
+    walls (a reflected zero momentum is -0) and supersonic states"""
+    hs = np.array([0.0, 0.005, 1.0, 10.0], np.float32)
+    hus = np.array([0.0, -0.0, 1e-30, -1e-30, 3.0, -3.0, 40.0, -40.0], np.float32)
+    bs = np.array([0.0, -0.0, 1.0], np.float32)
+    g = np.meshgrid(hs, hs, hus, hus, bs, bs, indexing="ij")
+    return [a.ravel().copy() for a in g]
+
+
+@pytest.mark.parametrize("name", ["hlle", "fwave", "augrie", "hybrid"])
+def test_signed_zero_edges(swe, oracle_mod, name):
+    ins = signed_zero_edges()
+    outs = gpu_edges(swe, SOLVERS[name], ins)
+    ref = oracle_mod.solve_edges(SOLVERS[name], *ins)
+    for o, r, k in zip(outs, ref, ("hUpdL", "hUpdR", "huUpdL", "huUpdR", "speed")):
+        assert_bitwise(o, r, k)
