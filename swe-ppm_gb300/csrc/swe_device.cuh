@@ -240,20 +240,11 @@ __device__ __forceinline__ float leftShare(float s) {
     return (s < -kZeroTol) ? 1.f : ((s > kZeroTol) ? 0.f : 0.5f);
 }
 
-/// f-wave (S = SOLVER_FWAVE) or HLLE (S = SOLVER_HLLE) net updates of one
-/// edge.  Wet/wet edges run straight through; an edge with a dry side takes
-/// the (warp-uniform away from shorelines) reflection branch.
+/// the two f-waves of an edge with both sides wet (or a dry side reflected):
+/// wave speeds, decomposition of the flux jump and routing
 template <int S>
-__device__ __forceinline__ void edgeFH(Cell L, Cell R, float &hUpdL, float &hUpdR, float &huUpdL, float &huUpdR,
-                                       float &speed) {
-    const bool dryL = L.h < kDryTol, dryR = R.h < kDryTol;
-    if (dryL || dryR) {
-        if (!reflectDry(L, R, dryL, dryR)) {
-            hUpdL = 0.f; hUpdR = 0.f; huUpdL = 0.f; huUpdR = 0.f;
-            speed = 0.f;
-            return;
-        }
-    }
+__device__ __forceinline__ void fhWaves(const Cell &L, const Cell &R, float &hUpdL, float &hUpdR, float &huUpdL,
+                                        float &huUpdR, float &speed) {
     float s1, s2;
     waveSpeeds<S>(L, R, s1, s2);
     const float df1 = R.hn - L.hn;
@@ -277,9 +268,28 @@ __device__ __forceinline__ void edgeFH(Cell L, Cell R, float &hUpdL, float &hUpd
         huUpdL = (0.f + w1 * z1u) + w2 * z2u;
         huUpdR = (0.f + (1.f - w1) * z1u) + (1.f - w2) * z2u;
     }
+    speed = fmaxf(fabsf(s1), fabsf(s2));
+}
+
+/// f-wave (S = SOLVER_FWAVE) or HLLE (S = SOLVER_HLLE) net updates of one
+/// edge.  Wet/wet edges run straight through; an edge with a dry side takes
+/// the (warp-uniform away from shorelines) reflection branch.
+template <int S>
+__device__ __forceinline__ void edgeFH(Cell L, Cell R, float &hUpdL, float &hUpdR, float &huUpdL, float &huUpdR,
+                                       float &speed) {
+    const bool dryL = L.h < kDryTol, dryR = R.h < kDryTol;
+    if (!(dryL || dryR)) {
+        fhWaves<S>(L, R, hUpdL, hUpdR, huUpdL, huUpdR, speed);
+        return;
+    }
+    if (!reflectDry(L, R, dryL, dryR)) {
+        hUpdL = 0.f; hUpdR = 0.f; huUpdL = 0.f; huUpdR = 0.f;
+        speed = 0.f;
+        return;
+    }
+    fhWaves<S>(L, R, hUpdL, hUpdR, huUpdL, huUpdR, speed);
     if (dryL) { hUpdL = 0.f; huUpdL = 0.f; }
     if (dryR) { hUpdR = 0.f; huUpdR = 0.f; }
-    speed = fmaxf(fabsf(s1), fabsf(s2));
 }
 
 /// max wave speed of one edge, bit-identical to edgeFH's `speed`
