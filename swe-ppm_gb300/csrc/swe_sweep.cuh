@@ -129,16 +129,17 @@ __device__ __forceinline__ float groupTimestep(const DomainDev &d, const GroupSt
 }
 
 /// per-cell quantities in x (normal momentum hu) and y (hv) direction:
-/// u = hu * (1/h), v = hv * (1/h), sqrt(h), sqrt(g) sqrt(h)
+/// u = hu * (1/h), v = hv * (1/h), sqrt(h), sqrt(g) sqrt(h).  Those of a dry
+/// cell are never read (an edge with a dry side solves with the mirrored wet
+/// side), so they are formed without a test.
 template <int S> __device__ __forceinline__ void cellQuantities(float h, float hu, float hv, float b, Cell &cx, Cell &cy) {
     float sq = 0.f, c = 0.f, ux = 0.f, uy = 0.f;
     if (S != SOLVER_AUGRIE) {
-        const bool wet = !(h < kDryTol);
         const float rh = 1.f / h;
         sq = sqrtf(h);
         if (S == SOLVER_HLLE) c = kSqrtG * sq;
-        ux = wet ? hu * rh : 0.f;
-        uy = wet ? hv * rh : 0.f;
+        ux = hu * rh;
+        uy = hv * rh;
     }
     cx = makeCell(h, hu, b, ux, sq, c);
     cy = makeCell(h, hv, b, uy, sq, c);
