@@ -295,12 +295,10 @@ __device__ __forceinline__ void edgeFH(Cell L, Cell R, float &hUpdL, float &hUpd
 /// max wave speed of one edge, bit-identical to edgeFH's `speed`
 template <int S> __device__ __forceinline__ float edgeSpeedFH(Cell L, Cell R) {
     const bool dryL = L.h < kDryTol, dryR = R.h < kDryTol;
-    float s1, s2;
-    if (!(dryL || dryR)) {  // wet / wet: no reflection
-        waveSpeeds<S>(L, R, s1, s2);
-        return fmaxf(fabsf(s1), fabsf(s2));
+    if (dryL || dryR) {
+        if (!reflectDry(L, R, dryL, dryR)) return 0.f;
     }
-    if (!reflectDry(L, R, dryL, dryR)) return 0.f;
+    float s1, s2;
     waveSpeeds<S>(L, R, s1, s2);
     return fmaxf(fabsf(s1), fabsf(s2));
 }
