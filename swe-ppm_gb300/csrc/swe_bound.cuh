@@ -102,18 +102,30 @@ __device__ __forceinline__ unsigned long long tileColumnsSpeed(const float *H, c
     const int xEnd = xb == I.nx + 1 ? xb + 1 : xb;    // (nx | nx+1) on the right rim
     // columns xa-1 .. xa+NB: the left neighbour, up to NB tile columns and the
     // right ghost column
-    float h[NB + 2], hu[NB + 2], hv[NB + 2], hB[NB], hvB[NB], hT[NB], hvT[NB];
+    float h[NB + 2], hu[NB + 2], hv[NB + 2];
 #pragma unroll
     for (int k = 0; k <= NB + 1; k++) {
         const int x = xa - 1 + k;
         const size_t o = size_t(x) * P + size_t(y);
         h[k] = 0.f; hu[k] = 0.f; hv[k] = 0.f;
         if (x < xEnd && active) { h[k] = H[o]; hu[k] = HU[o]; hv[k] = HV[o]; }
-        if (k > 0 && k <= NB) {
-            hB[k - 1] = 0.f; hvB[k - 1] = 0.f; hT[k - 1] = 0.f; hvT[k - 1] = 0.f;
-            if (x < xb && active) {
-                if (lane == 0) { hB[k - 1] = H[o - 1]; hvB[k - 1] = HV[o - 1]; }
-                if (top) { hT[k - 1] = H[o + 1]; hvT[k - 1] = HV[o + 1]; }
+    }
+    // the cell below the tile's first row (lanes 0 .. NB-1, column xa + lane)
+    // and, in the block's top rim tile, the ghost above its last row (lanes
+    // NB .. 2NB-1): loaded once per lane, handed to lane 0 / the top lane by
+    // shuffles (h and hv are all a y-edge needs)
+    float eh = 0.f, ehv = 0.f;
+    {
+        const int x = xa + (lane & (NB - 1));
+        if (x < xb) {
+            if (lane < NB) {
+                const size_t o = size_t(x) * P + size_t(I.y0 - 1);
+                eh = H[o];
+                ehv = HV[o];
+            } else if (lane < 2 * NB && I.y1 == I.ny + 1) {
+                const size_t o = size_t(x) * P + size_t(I.ny + 1);
+                eh = H[o];
+                ehv = HV[o];
             }
         }
     }
@@ -128,6 +140,9 @@ __device__ __forceinline__ unsigned long long tileColumnsSpeed(const float *H, c
         float hBl = __shfl_up_sync(0xffffffffu, h[k], 1);
         float hvBl = __shfl_up_sync(0xffffffffu, hv[k], 1);
         float wBl = __shfl_up_sync(0xffffffffu, w, 1);
+        const int kk = k <= NB ? k - 1 : 0;
+        const float eB = __shfl_sync(0xffffffffu, eh, kk), eBv = __shfl_sync(0xffffffffu, ehv, kk);
+        const float eT = __shfl_sync(0xffffffffu, eh, NB + kk), eTv = __shfl_sync(0xffffffffu, ehv, NB + kk);
         if (active) {
             if (!(vmax(wPrev, w) * kBoundMargin < T)) {  // x-edge (x-1 | x)
                 Cell L, R, dummy;
@@ -138,8 +153,8 @@ __device__ __forceinline__ unsigned long long tileColumnsSpeed(const float *H, c
             }
             if (k <= NB && x < xb) {                     // a column of the tile: its y-edges
                 if (lane == 0) {
-                    hBl = hB[k - 1];
-                    hvBl = hvB[k - 1];
+                    hBl = eB;
+                    hvBl = eBv;
                     wBl = cellSpeedBound(hBl, 0.f, hvBl);
                 }
                 if (!(vmax(wBl, w) * kBoundMargin < T)) {
@@ -149,10 +164,10 @@ __device__ __forceinline__ unsigned long long tileColumnsSpeed(const float *H, c
                     const float sy = edgeSpeed<S>(L, R);
                     if (sy > 0.f) best = umax64(best, speedKey(sy, edgeCode(tile, I, x, y, 1)));
                 }
-                if (top && !(vmax(w, cellSpeedBound(hT[k - 1], 0.f, hvT[k - 1])) * kBoundMargin < T)) {
+                if (top && !(vmax(w, cellSpeedBound(eT, 0.f, eTv)) * kBoundMargin < T)) {
                     Cell L, R, dummy;
                     cellQuantities<S>(h[k], hu[k], hv[k], 0.f, dummy, L);
-                    cellQuantities<S>(hT[k - 1], 0.f, hvT[k - 1], 0.f, dummy, R);
+                    cellQuantities<S>(eT, 0.f, eTv, 0.f, dummy, R);
                     const float st = edgeSpeed<S>(L, R);
                     if (st > 0.f) best = umax64(best, speedKey(st, edgeCode(tile, I, x, y + 1, 1)));
                 }
