@@ -241,8 +241,11 @@ __device__ __forceinline__ float leftShare(float s) {
 }
 
 /// the two f-waves of an edge with both sides wet (or a dry side reflected):
-/// wave speeds, decomposition of the flux jump and routing
-template <int S>
+/// wave speeds, decomposition of the flux jump and routing.  SWEEP: the caller
+/// only ever adds a left-going part to a right-going one (never -0: every such
+/// sum starts at +0) or to +0, so a subsonic edge may hand out its left-going
+/// parts without the + 0 that only turns -0 into +0
+template <int S, bool SWEEP = false>
 __device__ __forceinline__ void fhWaves(const Cell &L, const Cell &R, float &hUpdL, float &hUpdR, float &huUpdL,
                                         float &huUpdR, float &speed) {
     float s1, s2;
@@ -257,8 +260,8 @@ __device__ __forceinline__ void fhWaves(const Cell &L, const Cell &R, float &hUp
     const float z1u = beta1 * s1, z2u = beta2 * s2;
     // the routing of wave 1, then wave 2, into sums that start at +0
     if (s1 < -kZeroTol && s2 > kZeroTol) {  // subsonic: wave 1 left, wave 2 right
-        hUpdL = 0.f + beta1;
-        huUpdL = 0.f + z1u;
+        hUpdL = SWEEP ? beta1 : 0.f + beta1;
+        huUpdL = SWEEP ? z1u : 0.f + z1u;
         hUpdR = 0.f + beta2;
         huUpdR = 0.f + z2u;
     } else {
@@ -274,12 +277,12 @@ __device__ __forceinline__ void fhWaves(const Cell &L, const Cell &R, float &hUp
 /// f-wave (S = SOLVER_FWAVE) or HLLE (S = SOLVER_HLLE) net updates of one
 /// edge.  Wet/wet edges run straight through; an edge with a dry side takes
 /// the (warp-uniform away from shorelines) reflection branch.
-template <int S>
+template <int S, bool SWEEP = false>
 __device__ __forceinline__ void edgeFH(Cell L, Cell R, float &hUpdL, float &hUpdR, float &huUpdL, float &huUpdR,
                                        float &speed) {
     const bool dryL = L.h < kDryTol, dryR = R.h < kDryTol;
     if (!(dryL || dryR)) {
-        fhWaves<S>(L, R, hUpdL, hUpdR, huUpdL, huUpdR, speed);
+        fhWaves<S, SWEEP>(L, R, hUpdL, hUpdR, huUpdL, huUpdR, speed);
         return;
     }
     if (!reflectDry(L, R, dryL, dryR)) {
@@ -522,19 +525,19 @@ static __device__ __forceinline__ void edgeAugRie(float hL, float hR, float huL,
 /// shallower than 0.1 m, f-wave elsewhere
 constexpr float kHybridSwitchDepth = 0.1f;
 
-/// Full edge solve for any solver from per-cell quantities.
-template <int S>
+/// Full edge solve for any solver from per-cell quantities (SWEEP: see fhWaves).
+template <int S, bool SWEEP = false>
 __device__ __forceinline__ void edgeSolve(const Cell &L, const Cell &R, float &hUpdL, float &hUpdR, float &huUpdL,
                                           float &huUpdR, float &speed) {
     if (S == SOLVER_FWAVE || S == SOLVER_HLLE) {
-        edgeFH<S>(L, R, hUpdL, hUpdR, huUpdL, huUpdR, speed);
+        edgeFH<S, SWEEP>(L, R, hUpdL, hUpdR, huUpdL, huUpdR, speed);
     } else if (S == SOLVER_AUGRIE) {
         edgeAugRie(L.h, R.h, L.hn, R.hn, L.b, R.b, hUpdL, hUpdR, huUpdL, huUpdR, speed);
     } else {
         if (L.h < kHybridSwitchDepth || R.h < kHybridSwitchDepth)
             edgeAugRie(L.h, R.h, L.hn, R.hn, L.b, R.b, hUpdL, hUpdR, huUpdL, huUpdR, speed);
         else
-            edgeFH<SOLVER_FWAVE>(L, R, hUpdL, hUpdR, huUpdL, huUpdR, speed);
+            edgeFH<SOLVER_FWAVE, SWEEP>(L, R, hUpdL, hUpdR, huUpdL, huUpdR, speed);
     }
 }
 

@@ -442,7 +442,7 @@ __global__ void __launch_bounds__(kMaxTileRows, 4) sweepKernel(const DomainDev d
             cellQuantities<S>(H[o + 1], HU[o + 1], HV[o + 1], BT[o + 1], dummy, R);
             if (UPDATE) {
                 float aL, aR, auL, auR, s;
-                edgeSolve<S>(L, R, aL, aR, auL, auR, s);
+                edgeSolve<S, true>(L, R, aL, aR, auL, auR, s);
                 if (top) {
                     sTop[0][k] = aL;
                     sTop[1][k] = auL;
@@ -481,7 +481,7 @@ __global__ void __launch_bounds__(kMaxTileRows, 4) sweepKernel(const DomainDev d
             if (x >= x0 && active) {
                 if (UPDATE) {
                     float aL, aR, auL, auR, s;
-                    edgeSolve<S>(prevX, cx, aL, aR, auL, auR, s);
+                    edgeSolve<S, true>(prevX, cx, aL, aR, auL, auR, s);
                     if (x - 1 >= x0) {
                         float hn, hun, hvn;
                         if (SEM == SEM_UNSPLIT) {
@@ -556,7 +556,7 @@ __global__ void __launch_bounds__(kMaxTileRows, 4) sweepKernel(const DomainDev d
                                              sC[buf][3][t + 1], sC[buf][4][t + 1], sC[buf][5][t + 1]);
                     if (UPDATE) {
                         float bR, bRhv, s;
-                        edgeSolve<S>(cy, up, bLh, bR, bLhv, bRhv, s);
+                        edgeSolve<S, true>(cy, up, bLh, bR, bLhv, bRhv, s);
                         sR[buf][0][t + 1] = bR;
                         sR[buf][1][t + 1] = bRhv;
                     } else {
