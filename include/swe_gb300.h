@@ -103,7 +103,18 @@ typedef struct swe_gpu_desc {
                             intervals of this length (the drivers' -l; unsplit
                             step only; advanced with swe_gpu_lts_advance) */
     float duration;      /* simulated duration (local time stepping's last-step notice) */
+    int arithmetic;      /* SWE_ARITH_EXACT (0, default): IEEE division and square
+                            root, no contraction -- every solver and mode, results
+                            identical to the CPU restatement of the reference bit for
+                            bit.  SWE_ARITH_FAST: approximate reciprocal / square root
+                            and fused multiply-adds, results equal to FP32 round-off;
+                            offered for the f-wave and HLLE unsplit step with global
+                            time stepping (domains and ensembles), where a step is
+                            one launch that also computes the next maxTimestep. */
 } swe_gpu_desc;
+
+#define SWE_ARITH_EXACT 0
+#define SWE_ARITH_FAST 1
 
 int swe_gpu_domain_create(const swe_gpu_desc *desc, swe_gpu_domain **out);
 
@@ -120,7 +131,7 @@ typedef struct swe_gpu_instance {
  * persistent launches (swe_gpu_step, swe_gpu_advance; graph replay).  Block k
  * is instance k for uploads, downloads and snapshots.  From `options` only
  * solver, semantics, split_dt_mode, tile_rows, tile_cols, device,
- * kernel_variant and speed_pass are used.  The reference runs independent
+ * kernel_variant, speed_pass and arithmetic are used.  The reference runs independent
  * scenarios as separate processes; this has no counterpart there. */
 int swe_gpu_ensemble_create(const swe_gpu_instance *instances, int count, const swe_gpu_desc *options,
                             swe_gpu_domain **out);
@@ -242,6 +253,15 @@ int swe_gpu_launch_count(const swe_gpu_domain *dom, long long *count);
  * last pass evaluated edge by edge (both 0 when the full speed pass is in
  * use).  Synchronises the domain's stream. */
 int swe_gpu_speed_pass_stats(swe_gpu_domain *dom, int *tiles, int *evaluated);
+
+/* The fast step's pieces (SWE_ARITH_FAST): runs of next-state edges whose
+ * two cells are written by different work segments, evaluated for the next
+ * maxTimestep by the last of those segments to finish.  Five ints per piece:
+ * block, dir (0: x-edges (x0-1|x0) of rows y0 .. y0+len-1; 1: y-edges
+ * (y0-1|y0) of columns x0 .. x0+len-1), x0, y0, len.  Writes at most `cap`
+ * pieces to `out` (may be NULL with cap 0); *count = the number of pieces.
+ * Introspection for tests and tools; no counterpart in the reference. */
+int swe_gpu_fast_pieces(const swe_gpu_domain *dom, int *out, int cap, int *count);
 int swe_gpu_set_time(swe_gpu_domain *dom, float t);
 
 /* waits for everything queued on the domain (steps, transfers, async downloads) */

@@ -110,6 +110,32 @@ template <typename T> int ltsInterval(Domain<T> &D, double &tIO, int maxIteratio
 
 } // namespace
 
+/// CPU baseline: `nsteps` global steps of an unsplit multi-block domain with
+/// one OpenMP thread per block (the overdecomposed driver's parallel loops,
+/// src/examples/swe_mpi_overdecomp.cpp:269-323).  Returns the threads used.
+template <typename T> int stepParallel(Domain<T> &D, int nsteps, double *dts) {
+    const int nb = int(D.blocks.size());
+    int threads = 1;
+    for (int s = 0; s < nsteps; s++) {
+#pragma omp parallel for schedule(static)
+        for (int k = 0; k < nb; k++) D.blocks[k].applyBoundaryConditions();
+#pragma omp parallel for schedule(static)
+        for (int k = 0; k < nb; k++) D.exchangeGhosts(k);
+#pragma omp parallel for schedule(dynamic, 1)
+        for (int k = 0; k < nb; k++) D.blocks[k].timestepFromSpeed(D.blockSpeed(D.blocks[k]));
+        T dt = D.blocks[0].maxTimestep;
+        for (auto &B : D.blocks) dt = std::min(dt, B.maxTimestep);
+        for (auto &B : D.blocks) B.maxTimestep = dt;
+#pragma omp parallel for schedule(static)
+        for (int k = 0; k < nb; k++) D.blocks[k].updateUnsplit();
+        if (dts) dts[s] = double(dt);
+    }
+#ifdef _OPENMP
+    threads = omp_get_max_threads();
+#endif
+    return threads;
+}
+
 extern "C" {
 
 int oracle_solve_edges_f32(int solverId, int64_t n, const float *hL, const float *hR, const float *huL,
@@ -255,33 +281,10 @@ double oracle_domain_block_max_timestep(void *h, int k) {
     return H->f ? double(H->f->blocks[k].maxTimestep) : H->d->blocks[k].maxTimestep;
 }
 
-/// CPU baseline: `nsteps` global steps of an unsplit multi-block domain with
-/// one OpenMP thread per block (the overdecomposed driver's parallel loops,
-/// src/examples/swe_mpi_overdecomp.cpp:269-323).  Returns the threads used.
+/// stepParallel in the domain's precision
 int oracle_domain_step_parallel(void *h, int nsteps, double *dts) {
     auto *H = static_cast<Handle *>(h);
-    if (!H->f) return -1;
-    Domain<float> &D = *H->f;
-    const int nb = int(D.blocks.size());
-    int threads = 1;
-    for (int s = 0; s < nsteps; s++) {
-#pragma omp parallel for schedule(static)
-        for (int k = 0; k < nb; k++) D.blocks[k].applyBoundaryConditions();
-#pragma omp parallel for schedule(static)
-        for (int k = 0; k < nb; k++) D.exchangeGhosts(k);
-#pragma omp parallel for schedule(dynamic, 1)
-        for (int k = 0; k < nb; k++) D.blocks[k].timestepFromSpeed(D.blockSpeed(D.blocks[k]));
-        float dt = D.blocks[0].maxTimestep;
-        for (auto &B : D.blocks) dt = std::min(dt, B.maxTimestep);
-        for (auto &B : D.blocks) B.maxTimestep = dt;
-#pragma omp parallel for schedule(static)
-        for (int k = 0; k < nb; k++) D.blocks[k].updateUnsplit();
-        if (dts) dts[s] = double(dt);
-    }
-#ifdef _OPENMP
-    threads = omp_get_max_threads();
-#endif
-    return threads;
+    return H->f ? stepParallel(*H->f, nsteps, dts) : stepParallel(*H->d, nsteps, dts);
 }
 
 } // extern "C"

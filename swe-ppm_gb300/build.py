@@ -3,7 +3,8 @@
 CUDA sources are compiled for sm_103a only (one -gencode), in parallel, with
 -fmad=false (every fused multiply-add in the kernels is an explicit fmaf) and
 IEEE division / square root, so the kernels reproduce the CPU restatement bit
-for bit.  Host C++ (scenarios, initialisation, writer) is compiled with g++
+for bit.  The fast-arithmetic step (csrc/swe_fast.cu) is the exception: it is
+compiled with contraction and approximate division / square root.  Host C++ (scenarios, initialisation, writer) is compiled with g++
 -ffp-contract=off and linked into the same shared library.
 """
 import os
@@ -17,7 +18,12 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libswe_gb300.so")
 DRIVER = os.path.join(OUT, "swe_gb300")
 
-CUDA_SOURCES = ["csrc/swe_capi.cu", "csrc/swe_kernels_fh.cu", "csrc/swe_kernels_aug.cu", "csrc/swe_lts.cu", "csrc/swe_mlp.cu"]
+CUDA_SOURCES = ["csrc/swe_capi.cu", "csrc/swe_kernels_fh.cu", "csrc/swe_kernels_aug.cu", "csrc/swe_lts.cu", "csrc/swe_mlp.cu",
+                "csrc/swe_fast.cu"]
+# the fast-arithmetic step (SWE_ARITH_FAST) is its own translation unit with
+# contraction and approximate division and square root
+FAST_SOURCES = {"csrc/swe_fast.cu"}
+FAST_FLAGS = ["-fmad=true", "-prec-div=false", "-prec-sqrt=false", "-ftz=true"]
 HOST_SOURCES = ["host/swe_host.cpp", "host/netcdf_writer.cpp"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-fmad=false", "-lineinfo", "-std=c++17",
               "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-I" + os.path.join(ROOT, "include")]
@@ -59,7 +65,10 @@ def build(verbose=False, force=False):
     for src in CUDA_SOURCES:
         obj = os.path.join(OUT, os.path.basename(src) + ".o")
         objs.append(obj)
-        jobs.append([nvcc] + NVCC_FLAGS + ["-c", os.path.join(HERE, src), "-o", obj])
+        flags = NVCC_FLAGS
+        if src in FAST_SOURCES:
+            flags = [f for f in NVCC_FLAGS if f != "-fmad=false"] + FAST_FLAGS
+        jobs.append([nvcc] + flags + ["-c", os.path.join(HERE, src), "-o", obj])
     for src in HOST_SOURCES:
         obj = os.path.join(OUT, os.path.basename(src) + ".o")
         objs.append(obj)

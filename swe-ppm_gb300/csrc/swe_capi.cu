@@ -14,6 +14,7 @@
 #include "../../include/swe_gb300.h"
 #include "../../include/swe_gb300_mlp.h"
 #include "swe_device.cuh"
+#include "swe_fast.hpp"
 #include "swe_launch.hpp"
 #include "swe_mlp_launch.hpp"
 
@@ -302,6 +303,23 @@ struct swe_gpu_domain {
     cudaEvent_t upReady[2] = {nullptr, nullptr}, upConsumed[2] = {nullptr, nullptr};
     int upSlot = 0;
     bool upUsed[2] = {false, false};
+    // fast-arithmetic step (SWE_ARITH_FAST): one launch per step that also
+    // computes the next maxTimestep; dtValid = the groups' dt describes the
+    // current state (false after an upload or a bathymetry change, until a
+    // speed pass or a fast step has run)
+    bool fast = false;
+    bool dtValid = false;
+    std::vector<fast::Unit> unitsF;
+    std::vector<int> ctaSegF;
+    std::vector<fast::Piece> pieces;
+    std::vector<int> arrF;
+    int gridF = 0;
+    int tileRowsF = 256;          // rows per segment of the fast step (>= 64)
+    fast::Unit *dUnitsF = nullptr;
+    int *dCtaSegF = nullptr;
+    fast::Piece *dPieces = nullptr;
+    unsigned *dPieceCnt = nullptr;
+    int *dArrF = nullptr;
 };
 
 namespace {
@@ -372,9 +390,49 @@ int enqueueUpdate(swe_gpu_domain *D) {
     return SWE_GPU_OK;
 }
 
+/// the fast step's launch
+int enqueueFast(swe_gpu_domain *D) {
+    fast::FastDev f;
+    f.d = D->dev;
+    f.units = D->dUnitsF;
+    f.ctaSeg = D->dCtaSegF;
+    f.pieces = D->dPieces;
+    f.pieceCnt = D->dPieceCnt;
+    f.arr = D->dArrF;
+    CUDA_TRY(fast::launchFastStep(f, D->solver, D->gridF, D->tileRowsF, D->stream));
+    D->launches++;
+    D->ghostsValid = true;  // the step pushed the next ghost ring
+    D->dtValid = true;      // and computed the next maxTimestep
+    return SWE_GPU_OK;
+}
+
+/// fast arithmetic: the speed pass runs only when the groups' dt does not
+/// describe the current state (first step, after an upload)
+int enqueueFastPrologue(swe_gpu_domain *D) {
+    if (!D->ghostsValid) {
+        int rc = enqueueGhost(D, 0);
+        if (rc) return rc;
+        D->ghostsValid = true;
+    }
+    if (!D->dtValid) {
+        DomainDev d = D->dev;
+        d.units = D->dUnits;
+        d.ctaSeg = D->dCtaSeg;
+        CUDA_TRY(launchSpeed(d, D->grid, D->tileRows, D->stream));
+        D->launches++;
+        D->dtValid = true;
+    }
+    return SWE_GPU_OK;
+}
+
 /// one fused step; the ghost kernel runs only when the ghost ring is stale
 /// (after an upload), every update pass leaves a valid one behind
 int enqueueStep(swe_gpu_domain *D) {
+    if (D->fast) {
+        int rc = enqueueFastPrologue(D);
+        if (rc) return rc;
+        return enqueueFast(D);
+    }
     if (!D->ghostsValid) {
         int rc = enqueueGhost(D, 0);
         if (rc) return rc;
@@ -432,6 +490,11 @@ void freeDomain(swe_gpu_domain *D) {
     cudaFree(D->dCtaSeg);
     cudaFree(D->dUnitsU);
     cudaFree(D->dCtaSegU);
+    cudaFree(D->dUnitsF);
+    cudaFree(D->dCtaSegF);
+    cudaFree(D->dPieces);
+    cudaFree(D->dPieceCnt);
+    cudaFree(D->dArrF);
     cudaFree(D->dGroups);
     cudaFree(D->dTiles);
     cudaFree(D->dTileW);
@@ -488,7 +551,7 @@ struct BlockSpec {
 };
 
 struct DomainOptions {
-    int device, solver, semantics, splitDtMode, variant, tileRows, tileCols, speedPass;
+    int device, solver, semantics, splitDtMode, variant, tileRows, tileCols, speedPass, arithmetic;
     float ltsMaxTimestep, duration;
     int ngroups;
 };
@@ -555,6 +618,137 @@ void buildPartitions(swe_gpu_domain *D, int tileColsArg) {
     }
 }
 
+/// Partition and pieces of the fast step (swe_fast.cu).  Segments: the
+/// (row tile, column) pairs of all blocks split evenly over a persistent
+/// grid sized from the kernel's occupancy, as for the update pass.  Pieces:
+/// each segment's left edge column (x0-1 | x0) and bottom edge row
+/// (y0-1 | y0) where the cell across belongs to another segment (the
+/// neighbouring segment of the tile, the tile below, or the neighbour block
+/// that fills this block's ghost column / row); every segment writing one of
+/// the piece's cells arrives on it.  Returns false when blocks that share a
+/// side differ in the length of that side (the pieces would not line up).
+bool buildFastPlan(swe_gpu_domain *D) {
+    D->unitsF.clear();
+    D->ctaSegF.clear();
+    D->pieces.clear();
+    D->arrF.clear();
+    const int TY = std::max(64, D->tileRows);
+    D->tileRowsF = TY;
+    int sms = 148;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, D->device);
+    const int occ = std::max(1, std::min(16, fast::fastOccupancy(D->solver, TY)));
+    long long total = 0;
+    for (const BlockDesc &B : D->blocks) total += (long long)((B.ny + TY - 1) / TY) * B.nx;
+    long long workers = (long long)sms * occ;
+    if (D->tileColsArg > 0) workers = std::max(workers, (total + D->tileColsArg - 1) / D->tileColsArg);
+    workers = std::max(1LL, std::min(total, workers));
+    D->gridF = int(workers);
+    const int cap = D->tileColsArg > 0 ? std::min(D->tileColsArg, kMaxTileCols) : kMaxTileCols;
+    D->ctaSegF.assign(1, 0);
+    long long pos = 0;
+    int k = 0, tile = 0, col = 1;
+    auto tilesOf = [&](int kk) { return (D->blocks[kk].ny + TY - 1) / TY; };
+    for (long long c = 0; c < workers; c++) {
+        const long long end = total * (c + 1) / workers;
+        while (pos < end) {
+            const BlockDesc &B = D->blocks[k];
+            const long long take = std::min<long long>(end - pos, (long long)(B.nx + 1 - col));
+            const int len = int(std::min<long long>(take, cap));
+            D->unitsF.push_back(fast::Unit{k, 1 + tile * TY, col, col + len, 0, 0});
+            pos += len;
+            col += len;
+            if (col > B.nx) {
+                col = 1;
+                if (++tile >= tilesOf(k)) {
+                    tile = 0;
+                    k++;
+                }
+            }
+        }
+        D->ctaSegF.push_back(int(D->unitsF.size()));
+    }
+    // segments of every (block, tile) in column order
+    std::vector<std::vector<std::vector<int>>> segsOf(D->blocks.size());
+    for (size_t b = 0; b < D->blocks.size(); b++) segsOf[b].resize(tilesOf(int(b)));
+    for (int s = 0; s < int(D->unitsF.size()); s++) {
+        const fast::Unit &u = D->unitsF[s];
+        segsOf[u.block][(u.y0 - 1) / TY].push_back(s);
+    }
+    auto covering = [&](int blk, int ti, int xa, int xb, std::vector<int> &out) {
+        for (int s : segsOf[blk][ti]) {
+            const fast::Unit &u = D->unitsF[s];
+            if (u.x0 < xb && xa < u.x1) out.push_back(s);
+        }
+    };
+    std::vector<std::vector<int>> arrOf(D->unitsF.size());
+    for (int s = 0; s < int(D->unitsF.size()); s++) {
+        const fast::Unit u = D->unitsF[s];
+        const BlockDesc &B = D->blocks[u.block];
+        const int ti = (u.y0 - 1) / TY;
+        const int yTop = std::min(u.y0 + TY - 1, B.ny);
+        if (u.x0 > 1 || B.bnd[0] == CONNECT_WITHIN_RANK) {
+            std::vector<int> c{s};
+            if (u.x0 > 1) {
+                covering(u.block, ti, u.x0 - 1, u.x0, c);
+            } else {
+                const int nb = B.nbr[0];
+                if (D->blocks[nb].ny != B.ny) return false;
+                covering(nb, ti, D->blocks[nb].nx, D->blocks[nb].nx + 1, c);
+            }
+            const int id = int(D->pieces.size());
+            D->pieces.push_back(fast::Piece{u.block, 0, u.x0, u.y0, yTop - u.y0 + 1, int(c.size())});
+            for (int x : c) arrOf[x].push_back(id);
+        }
+        if (u.y0 > 1 || B.bnd[2] == CONNECT_WITHIN_RANK) {
+            std::vector<int> c{s};
+            if (u.y0 > 1) {
+                covering(u.block, ti - 1, u.x0, u.x1, c);
+            } else {
+                const int nb = B.nbr[2];
+                if (D->blocks[nb].nx != B.nx) return false;
+                covering(nb, tilesOf(nb) - 1, u.x0, u.x1, c);
+            }
+            const int id = int(D->pieces.size());
+            D->pieces.push_back(fast::Piece{u.block, 1, u.x0, u.y0, u.x1 - u.x0, int(c.size())});
+            for (int x : c) arrOf[x].push_back(id);
+        }
+    }
+    for (int s = 0; s < int(D->unitsF.size()); s++) {
+        if (int(arrOf[s].size()) > std::min(fast::kMaxArrivals, TY / fast::fastRows())) return false;
+        D->unitsF[s].arrBegin = int(D->arrF.size());
+        D->arrF.insert(D->arrF.end(), arrOf[s].begin(), arrOf[s].end());
+        D->unitsF[s].arrEnd = int(D->arrF.size());
+    }
+    return true;
+}
+
+/// device copies of the fast step's plan (replacing earlier ones)
+int uploadFastPlan(swe_gpu_domain *D) {
+    cudaFree(D->dUnitsF);
+    cudaFree(D->dCtaSegF);
+    cudaFree(D->dPieces);
+    cudaFree(D->dPieceCnt);
+    cudaFree(D->dArrF);
+    D->dUnitsF = nullptr;
+    D->dCtaSegF = nullptr;
+    D->dPieces = nullptr;
+    D->dPieceCnt = nullptr;
+    D->dArrF = nullptr;
+    const size_t np = std::max<size_t>(1, D->pieces.size()), na = std::max<size_t>(1, D->arrF.size());
+    CUDA_TRY(cudaMalloc(&D->dUnitsF, sizeof(fast::Unit) * D->unitsF.size()));
+    CUDA_TRY(cudaMalloc(&D->dCtaSegF, sizeof(int) * D->ctaSegF.size()));
+    CUDA_TRY(cudaMalloc(&D->dPieces, sizeof(fast::Piece) * np));
+    CUDA_TRY(cudaMalloc(&D->dPieceCnt, sizeof(unsigned) * np));
+    CUDA_TRY(cudaMalloc(&D->dArrF, sizeof(int) * na));
+    CUDA_TRY(cudaMemcpy(D->dUnitsF, D->unitsF.data(), sizeof(fast::Unit) * D->unitsF.size(), cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(D->dCtaSegF, D->ctaSegF.data(), sizeof(int) * D->ctaSegF.size(), cudaMemcpyHostToDevice));
+    if (!D->pieces.empty())
+        CUDA_TRY(cudaMemcpy(D->dPieces, D->pieces.data(), sizeof(fast::Piece) * D->pieces.size(), cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemset(D->dPieceCnt, 0, sizeof(unsigned) * np));
+    if (!D->arrF.empty()) CUDA_TRY(cudaMemcpy(D->dArrF, D->arrF.data(), sizeof(int) * D->arrF.size(), cudaMemcpyHostToDevice));
+    return SWE_GPU_OK;
+}
+
 /// per-group work counts of the passes
 void groupCounts(swe_gpu_domain *D, std::vector<GroupState> &g) {
     for (GroupState &x : g) {
@@ -564,6 +758,8 @@ void groupCounts(swe_gpu_domain *D, std::vector<GroupState> &g) {
     }
     for (const WorkUnit &u : D->units) g[D->blocks[u.block].group].units++;
     for (const WorkUnit &u : D->unitsU) g[D->blocks[u.block].group].unitsUpd++;
+    for (GroupState &x : g) x.unitsFast = 0;
+    for (const fast::Unit &u : D->unitsF) g[D->blocks[u.block].group].unitsFast++;
     for (const TileInfo &t : D->tiles) g[t.group].tiles++;
 }
 
@@ -618,9 +814,15 @@ int buildDomain(const std::vector<BlockSpec> &spec, const DomainOptions &o, swe_
         D->maxPerimeter = std::max(D->maxPerimeter, 2 * B.nx + 2 * B.ny + 4);
         D->blocks.push_back(B);
     }
-    elems += 32;  // slack so the last column's padding stays inside the allocation
+    elems += 32;  // slack so the last column's padding (and the fast step's strip copies) stays inside the allocation
     D->fieldElems = elems;
     buildPartitions(D, tileColsArg);
+    D->fast = o.arithmetic == SWE_ARITH_FAST;
+    if (D->fast && !buildFastPlan(D)) {
+        if (D->ownStream) cudaStreamDestroy(D->ownStream);
+        delete D;
+        return fail(SWE_GPU_ERR_INVALID, "fast arithmetic: neighbouring blocks must share the length of their common side");
+    }
     // Bounded speed pass: bound tiles of 32 x 32 cells per block, numbered
     // block by block, column of tiles by column of tiles
     bool smallBlocks = true;
@@ -630,7 +832,7 @@ int buildDomain(const std::vector<BlockSpec> &spec, const DomainOptions &o, swe_
     // pass, one streaming read of every edge, is faster)
     D->bounded = D->variant == VARIANT_TILE && D->semantics == SEM_UNSPLIT &&
                  (D->solver == SOLVER_FWAVE || D->solver == SOLVER_HLLE) && o.speedPass == 0 && smallBlocks &&
-                 !D->lts;
+                 !D->lts && !D->fast;
     if (D->bounded) {
         int base = 0;
         for (BlockDesc &B : D->blocks) {
@@ -768,6 +970,13 @@ int buildDomain(const std::vector<BlockSpec> &spec, const DomainOptions &o, swe_
         freeDomain(D);
         return fail(SWE_GPU_ERR_CUDA, "domain initialisation: %s", cudaGetErrorString(e));
     }
+    if (D->fast) {
+        const int rcF = uploadFastPlan(D);
+        if (rcF) {
+            freeDomain(D);
+            return rcF;
+        }
+    }
     for (int i = 0; i < 2; i++) {
         D->dev.h[i] = D->h[i];
         D->dev.hu[i] = D->hu[i];
@@ -815,6 +1024,18 @@ int checkCommon(int solver, int semantics, const int boundary[4]) {
     return SWE_GPU_OK;
 }
 
+int checkArithmetic(int arithmetic, int solver, int semantics, bool lts, int kernelVariant) {
+    if (arithmetic == SWE_ARITH_EXACT) return SWE_GPU_OK;
+    if (arithmetic != SWE_ARITH_FAST) return fail(SWE_GPU_ERR_INVALID, "unknown arithmetic %d", arithmetic);
+    if (solver != SWE_SOLVER_FWAVE && solver != SWE_SOLVER_HLLE)
+        return fail(SWE_GPU_ERR_INVALID, "fast arithmetic is offered for the f-wave and HLLE solvers");
+    if (semantics != SWE_SEMANTICS_UNSPLIT)
+        return fail(SWE_GPU_ERR_INVALID, "fast arithmetic is offered for the unsplit step");
+    if (lts) return fail(SWE_GPU_ERR_INVALID, "fast arithmetic is offered with global time stepping");
+    if (kernelVariant != 0) return fail(SWE_GPU_ERR_INVALID, "fast arithmetic uses the CTA-tile mapping (kernel_variant 0)");
+    return SWE_GPU_OK;
+}
+
 int checkTiles(int tileRows, int tileCols) {
     const int tr = tileRows > 0 ? tileRows : 256;
     if (tr % 32 != 0 || tr > kMaxTileRows) return fail(SWE_GPU_ERR_INVALID, "tile_rows must be a multiple of 32 <= %d", kMaxTileRows);
@@ -844,6 +1065,8 @@ int swe_gpu_domain_create(const swe_gpu_desc *desc, swe_gpu_domain **out) {
     rc = checkTiles(desc->tile_rows, desc->tile_cols);
     if (rc) return rc;
     const bool lts = desc->lts_max_timestep > 0.f;
+    rc = checkArithmetic(desc->arithmetic, desc->solver, desc->semantics, lts, desc->kernel_variant);
+    if (rc) return rc;
     std::vector<BlockSpec> spec;
     for (int k = 0; k < bx * by; k++) {
         const int px = k / by, py = k % by;
@@ -872,6 +1095,7 @@ int swe_gpu_domain_create(const swe_gpu_desc *desc, swe_gpu_domain **out) {
     o.speedPass = desc->speed_pass;
     o.ltsMaxTimestep = desc->lts_max_timestep;
     o.duration = desc->duration;
+    o.arithmetic = desc->arithmetic;
     o.ngroups = lts ? bx * by : 1;
     return buildDomain(spec, o, out);
 }
@@ -883,6 +1107,8 @@ int swe_gpu_ensemble_create(const swe_gpu_instance *inst, int count, const swe_g
     if (options->lts_max_timestep > 0.f)
         return fail(SWE_GPU_ERR_INVALID, "ensembles step globally per instance (no local time stepping)");
     int rc = checkTiles(options->tile_rows, options->tile_cols);
+    if (rc) return rc;
+    rc = checkArithmetic(options->arithmetic, options->solver, options->semantics, false, options->kernel_variant);
     if (rc) return rc;
     std::vector<BlockSpec> spec;
     for (int i = 0; i < count; i++) {
@@ -914,6 +1140,7 @@ int swe_gpu_ensemble_create(const swe_gpu_instance *inst, int count, const swe_g
     o.tileRows = options->tile_rows;
     o.tileCols = options->tile_cols;
     o.speedPass = options->speed_pass;
+    o.arithmetic = options->arithmetic;
     o.ngroups = count;
     return buildDomain(spec, o, out);
 }
@@ -983,6 +1210,7 @@ static int stageTransfer(swe_gpu_domain *D, int firstBlock, int nblocks, float *
         CUDA_TRY(cudaGetLastError());
         D->launches++;
         D->ghostsValid = false;
+        D->dtValid = false;
     }
     if (wait) CUDA_TRY(cudaStreamSynchronize(D->stream));
     return SWE_GPU_OK;
@@ -1055,6 +1283,7 @@ int swe_gpu_upload_domain_async(swe_gpu_domain *dom, const float *h, const float
     CUDA_TRY(cudaEventRecord(dom->upConsumed[j], dom->stream));
     dom->upUsed[j] = true;
     dom->ghostsValid = false;
+    dom->dtValid = false;
     return SWE_GPU_OK;
 }
 
@@ -1138,6 +1367,7 @@ int swe_gpu_free_pinned(void *p) {
 int swe_gpu_exchange_bathymetry(swe_gpu_domain *dom) {
     if (!dom) return fail(SWE_GPU_ERR_INVALID, "null domain handle");
     CUDA_TRY(cudaSetDevice(dom->device));
+    dom->dtValid = false;
     return enqueueGhost(dom, 1);
 }
 
@@ -1156,6 +1386,9 @@ int swe_gpu_compute_fluxes(swe_gpu_domain *dom) {
     if (dom && dom->lts) return fail(SWE_GPU_ERR_INVALID, "local-time-stepping domain: use swe_gpu_lts_advance");
     if (!dom) return fail(SWE_GPU_ERR_INVALID, "null domain handle");
     CUDA_TRY(cudaSetDevice(dom->device));
+    // fast arithmetic: the previous step already computed this state's
+    // maxTimestep; a speed pass runs only when it did not
+    if (dom->fast) return enqueueFastPrologue(dom);
     return enqueueSpeed(dom);
 }
 
@@ -1164,6 +1397,11 @@ int swe_gpu_update_unknowns(swe_gpu_domain *dom, float dt) {
     if (dom && dom->lts) return fail(SWE_GPU_ERR_INVALID, "local-time-stepping domain: use swe_gpu_lts_advance");
     if (!dom) return fail(SWE_GPU_ERR_INVALID, "null domain handle");
     CUDA_TRY(cudaSetDevice(dom->device));
+    if (dom->fast) {
+        int rc = enqueueFastPrologue(dom);
+        if (rc) return rc;
+        return enqueueFast(dom);
+    }
     return enqueueUpdate(dom);
 }
 
@@ -1193,6 +1431,10 @@ int swe_gpu_advance(swe_gpu_domain *dom, float t_end, int max_steps, int *steps_
     if (dom->lts) return fail(SWE_GPU_ERR_INVALID, "local-time-stepping domain: use swe_gpu_lts_advance");
     CUDA_TRY(cudaSetDevice(dom->device));
     const int batch = 16;
+    if (dom->fast) {  // fast step: ghost ring and dt of the current state first, outside the graph
+        int rc0 = enqueueFastPrologue(dom);
+        if (rc0) return rc0;
+    }
     if (!dom->graph) {  // capture `batch` steps once; replays are identical
         cudaGraph_t g;
         CUDA_TRY(cudaStreamBeginCapture(dom->stream, cudaStreamCaptureModeThreadLocal));
@@ -1410,6 +1652,13 @@ int swe_gpu_retile(swe_gpu_domain *dom, int tile_rows, int tile_cols) {
     dom->dev.units = dom->dUnits;
     dom->dev.ctaSeg = dom->dCtaSeg;
     dom->dev.tileRows = dom->tileRows;
+    if (dom->fast) {
+        if (!buildFastPlan(dom)) return fail(SWE_GPU_ERR_INVALID, "fast arithmetic: pieces do not line up");
+        rc = uploadFastPlan(dom);
+        if (rc) return rc;
+        groupCounts(dom, g);
+        CUDA_TRY(cudaMemcpy(dom->dGroups, g.data(), sizeof(GroupState) * g.size(), cudaMemcpyHostToDevice));
+    }
     // captured step graphs hold the old launch shapes
     if (dom->graph) cudaGraphExecDestroy(dom->graph);
     if (dom->ltsGraph) cudaGraphExecDestroy(dom->ltsGraph);
@@ -1449,7 +1698,7 @@ int swe_gpu_autotune(swe_gpu_domain *dom, int trial_steps, int *best_rows, int *
         release();
         return fail(SWE_GPU_ERR_NOMEM, "tuner: no room for a copy of the state");
     }
-    const bool ghostsValid = dom->ghostsValid;
+    const bool ghostsValid = dom->ghostsValid, dtValid = dom->dtValid;
     auto copyState = [&](bool toSave) -> cudaError_t {
         for (int i = 0; i < 6; i++) {
             cudaError_t e = cudaMemcpyAsync(toSave ? save[i] : live[i], toSave ? live[i] : save[i], bytes,
@@ -1467,6 +1716,7 @@ int swe_gpu_autotune(swe_gpu_domain *dom, int trial_steps, int *best_rows, int *
         }
         if (e == cudaSuccess) e = cudaStreamSynchronize(dom->stream);
         dom->ghostsValid = ghostsValid;
+        dom->dtValid = dtValid;
         if (e == cudaSuccess && !toSave) {
             // the saved group states carry the saved partition's segment counts
             std::vector<GroupState> g(dom->ngroups);
@@ -1543,6 +1793,18 @@ int swe_gpu_speed_pass_stats(swe_gpu_domain *dom, int *tiles, int *evaluated) {
     }
     if (tiles) *tiles = dom->bounded ? t : 0;
     if (evaluated) *evaluated = dom->bounded ? e : 0;
+    return SWE_GPU_OK;
+}
+
+int swe_gpu_fast_pieces(const swe_gpu_domain *dom, int *out, int cap, int *count) {
+    if (!dom || !count || cap < 0 || (cap > 0 && !out)) return fail(SWE_GPU_ERR_INVALID, "bad argument");
+    if (!dom->fast) return fail(SWE_GPU_ERR_INVALID, "not a fast-arithmetic domain");
+    *count = int(dom->pieces.size());
+    for (int i = 0; i < std::min(cap, *count); i++) {
+        const fast::Piece &p = dom->pieces[i];
+        const int v[5] = {p.block, p.dir, p.x0, p.y0, p.len};
+        for (int j = 0; j < 5; j++) out[5 * i + j] = v[j];
+    }
     return SWE_GPU_OK;
 }
 

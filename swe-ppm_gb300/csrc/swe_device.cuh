@@ -120,6 +120,7 @@ struct __align__(128) GroupState {
     long long prevA, prevB;
     int prevDir, prevValid;
     int lastCandidates;      // tiles the last bounded speed pass evaluated edge by edge
+    int unitsFast;           // segments of the fast-arithmetic step in this group
 };
 
 // Bound tile of the bounded speed pass: 32 x 32 interior cells of a block,

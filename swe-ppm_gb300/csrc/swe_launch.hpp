@@ -26,6 +26,22 @@ inline cudaError_t launchPdl(void (*k)(P...), dim3 grid, dim3 block, cudaStream_
     return cudaLaunchKernelEx(&cfg, k, args...);
 }
 
+/// launchPdl with dynamic shared memory
+template <class... P, class... A>
+inline cudaError_t launchPdlSmem(void (*k)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, A... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k, args...);
+}
+
 // speed pass (computeNumericalFluxes' wave speeds + maxTimestep) and fused
 // solve-and-update pass (updateUnknowns) of the f-wave and HLLE solvers
 cudaError_t launchSpeedFH(const DomainDev &d, int nunits, int threads, cudaStream_t s);

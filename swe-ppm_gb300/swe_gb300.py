@@ -21,6 +21,7 @@ LIB_PATH = os.path.join(HERE, "_build", "libswe_gb300.so")
 FWAVE, AUGRIE, HYBRID, HLLE = 1, 2, 3, 4
 SOLVERS = {"fwave": FWAVE, "augrie": AUGRIE, "hybrid": HYBRID, "hlle": HLLE}
 UNSPLIT, SPLIT = 0, 1
+EXACT, FAST = 0, 1  # arithmetic of the step (swe_gpu_desc.arithmetic)
 SPLIT_DT_MAX, SPLIT_DT_LAST_EDGE = 0, 1
 OUTFLOW, WALL, INFLOW, CONNECT, CONNECT_WITHIN_RANK, PASSIVE = range(6)
 
@@ -44,7 +45,7 @@ EXPORTED = [
     "swe_gpu_snapshot_slabs_async", "swe_gpu_snapshot_wait", "swe_gpu_alloc_pinned", "swe_gpu_free_pinned",
     "swe_gpu_launch_count", "swe_gpu_speed_pass_stats", "swe_gpu_lts_advance", "swe_gpu_lts_state", "swe_gpu_lts_blocks",
     "swe_gpu_block_steps", "swe_gpu_ensemble_create", "swe_gpu_group_count", "swe_gpu_group_state",
-    "swe_gpu_retile", "swe_gpu_autotune",
+    "swe_gpu_retile", "swe_gpu_autotune", "swe_gpu_fast_pieces",
     "swe_mlp_last_error", "swe_mlp_gemm_check", "swe_mlp_param_count", "swe_mlp_create", "swe_mlp_destroy",
     "swe_mlp_get_params", "swe_mlp_set_params", "swe_mlp_forward", "swe_mlp_solve", "swe_mlp_loss_grad",
     "swe_mlp_train", "swe_gpu_surrogate_step", "swe_gpu_surrogate_edge_count", "swe_gpu_log_edges",
@@ -64,7 +65,7 @@ class Desc(C.Structure):
                 ("boundary", C.c_int * 4), ("solver", C.c_int), ("semantics", C.c_int),
                 ("split_dt_mode", C.c_int), ("tile_rows", C.c_int), ("tile_cols", C.c_int), ("device", C.c_int),
                 ("kernel_variant", C.c_int), ("speed_pass", C.c_int), ("lts_max_timestep", C.c_float),
-                ("duration", C.c_float)]
+                ("duration", C.c_float), ("arithmetic", C.c_int)]
 
 
 class Instance(C.Structure):
@@ -111,6 +112,7 @@ def lib():
         L.swe_gpu_get_time.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_int)]
         L.swe_gpu_launch_count.argtypes = [vp, C.POINTER(C.c_longlong)]
         L.swe_gpu_speed_pass_stats.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        L.swe_gpu_fast_pieces.argtypes = [vp, C.c_void_p, C.c_int, C.POINTER(C.c_int)]
         L.swe_gpu_lts_advance.argtypes = [vp, C.c_float, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_float)]
         L.swe_gpu_lts_state.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_int), C.POINTER(C.c_int), vp]
         L.swe_gpu_lts_blocks.argtypes = [vp, vp, vp]
@@ -244,7 +246,7 @@ class Domain:
 
     def __init__(self, nx_cols, ny_rows, dx, dy, boundary=(OUTFLOW,) * 4, solver=HLLE, semantics=UNSPLIT,
                  split_dt_mode=SPLIT_DT_MAX, tile_rows=0, tile_cols=0, device=0, kernel_variant=0, speed_pass=0,
-                 lts_max_timestep=0.0, duration=0.0):
+                 lts_max_timestep=0.0, duration=0.0, arithmetic=0):
         self.nx_cols = [int(v) for v in nx_cols]
         self.ny_rows = [int(v) for v in ny_rows]
         self.bx, self.by = len(self.nx_cols), len(self.ny_rows)
@@ -262,6 +264,7 @@ class Domain:
         d.kernel_variant = int(kernel_variant)
         d.speed_pass = int(speed_pass)
         d.lts_max_timestep, d.duration = float(lts_max_timestep), float(duration)
+        d.arithmetic = int(arithmetic)
         self.handle = C.c_void_p()
         _check(lib().swe_gpu_domain_create(C.byref(d), C.byref(self.handle)))
         self.shapes = [(self.nx_cols[k // self.by], self.ny_rows[k % self.by]) for k in range(self.bx * self.by)]
@@ -449,6 +452,14 @@ class Domain:
         _check(lib().swe_gpu_speed_pass_stats(self.handle, C.byref(t), C.byref(e)))
         return t.value, e.value
 
+    def fast_pieces(self):
+        """the fast step's pieces: rows of (block, dir, x0, y0, len)"""
+        n = C.c_int()
+        _check(lib().swe_gpu_fast_pieces(self.handle, None, 0, C.byref(n)))
+        out = np.zeros((max(1, n.value), 5), dtype=np.int32)
+        _check(lib().swe_gpu_fast_pieces(self.handle, _p(out), n.value, C.byref(n)))
+        return out[:n.value]
+
     def set_time(self, t):
         _check(lib().swe_gpu_set_time(self.handle, float(t)))
 
@@ -482,7 +493,7 @@ class Ensemble(Domain):
     boundaries and dt) stepped together in one handle.  Block k = instance k."""
 
     def __init__(self, instances, solver=HLLE, semantics=UNSPLIT, split_dt_mode=SPLIT_DT_MAX, tile_rows=0,
-                 tile_cols=0, device=0, kernel_variant=0, speed_pass=0):
+                 tile_cols=0, device=0, kernel_variant=0, speed_pass=0, arithmetic=0):
         n = len(instances)
         arr = (Instance * n)()
         for i, (nx, ny, dx, dy, bnd) in enumerate(instances):
@@ -493,6 +504,7 @@ class Ensemble(Domain):
         d.solver, d.semantics, d.split_dt_mode = int(solver), int(semantics), int(split_dt_mode)
         d.tile_rows, d.tile_cols, d.device = int(tile_rows), int(tile_cols), int(device)
         d.kernel_variant, d.speed_pass = int(kernel_variant), int(speed_pass)
+        d.arithmetic = int(arithmetic)
         self.handle = C.c_void_p()
         _check(lib().swe_gpu_ensemble_create(arr, n, C.byref(d), C.byref(self.handle)))
         self.bx, self.by = n, 1
