@@ -119,19 +119,106 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def setup_domain(swe, device, n=N_CELLS_SIDE, solver=None):
+def setup_domain(swe, device, n=N_CELLS_SIDE, solver=None, arithmetic=None):
     solver = swe.HLLE if solver is None else solver
+    arithmetic = swe.FAST if arithmetic is None else arithmetic
     geo, h, hu, hv, b = swe.init_domain(swe.SCENARIO_TSUNAMI, n, n, N_BLOCKS, [n, SEED, 100000.0])
     tile_rows = int(os.environ.get("SWE_TILE_ROWS", "0"))
     tile_cols = int(os.environ.get("SWE_TILE_COLS", "0"))
-    variant = int(os.environ.get("SWE_KERNEL_VARIANT", "0"))
     speed_pass = int(os.environ.get("SWE_SPEED_PASS", "0"))  # 1: evaluate every edge in the speed pass
     D = swe.Domain(geo["nx_cols"], geo["ny_rows"], geo["dx"], geo["dy"], boundary=geo["boundary"], solver=solver,
-                   tile_rows=tile_rows, tile_cols=tile_cols, device=device, kernel_variant=variant,
-                   speed_pass=speed_pass)
+                   tile_rows=tile_rows, tile_cols=tile_cols, device=device, speed_pass=speed_pass,
+                   arithmetic=arithmetic)
     D.upload(h, hu, hv, b)
     D.exchange_bathymetry()
     return D, geo, (h, hu, hv, b)
+
+
+def timed_steps(D, stream, flush, steps):
+    """`steps` steps, L2 flushed before each, CUDA events around each step on
+    the library's stream; returns the milliseconds of every step"""
+    import torch
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    with torch.cuda.stream(stream):
+        for e0, e1 in ev:
+            flush.zero_()
+            e0.record(stream)
+            D.step(1)
+            e1.record(stream)
+    stream.synchronize()
+    return [e0.elapsed_time(e1) for e0, e1 in ev]
+
+
+def kernel_times(D, stream, flush, steps):
+    """the reference's call sequence, L2 flushed before each step, events
+    between the calls: mean ms of setGhostLayer, computeNumericalFluxes and
+    updateUnknowns (the fast step: the ghost ring and the dt come from the
+    previous launch, so the first two launch nothing)"""
+    import torch
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(steps)]
+    with torch.cuda.stream(stream):
+        for e in ev:
+            flush.zero_()
+            e[0].record(stream)
+            D.set_ghost_layer()
+            e[1].record(stream)
+            D.compute_fluxes()
+            e[2].record(stream)
+            D.update_unknowns()
+            e[3].record(stream)
+    stream.synchronize()
+    return {k: statistics.mean(e[i].elapsed_time(e[i + 1]) for e in ev) for i, k in
+            enumerate(("ghost", "speed", "update"))}
+
+
+def accuracy_measure(swe, device, steps=100):
+    """Error of the GPU steps against the FP64 oracle of the same scheme on
+    the benchmark's workload (2048^2 tsunami, HLLE, unsplit), after `steps`
+    steps from the initial state: relative L1 and max |dh| of the fast step,
+    of the bit-exact step (identical to the FP32 oracle, the reference's own
+    float arithmetic), and mass drift in FP64 of all three.  The tsunami stays
+    wet (no dry clamp) and its bump does not reach the outflow sides in this
+    time, so mass is conserved up to round-off."""
+    import oracle
+    oracle.build()
+    out = {}
+    geo, h, hu, hv, b = swe.init_domain(swe.SCENARIO_TSUNAMI, N_CELLS_SIDE, N_CELLS_SIDE, N_BLOCKS,
+                                        [N_CELLS_SIDE, SEED, 100000.0])
+    m = []
+    off = 0
+    for k in range(len(geo["nx_cols"]) * len(geo["ny_rows"])):
+        nx, ny = geo["nx_cols"][k // len(geo["ny_rows"])], geo["ny_rows"][k % len(geo["ny_rows"])]
+        a = np.zeros((nx + 2, ny + 2), bool)
+        a[1:-1, 1:-1] = True
+        m.append(a.ravel())
+    m = np.concatenate(m)
+    states = {}
+    for name, arith in (("fast", swe.FAST), ("exact", swe.EXACT)):
+        D = swe.Domain(geo["nx_cols"], geo["ny_rows"], geo["dx"], geo["dy"], boundary=geo["boundary"],
+                       solver=swe.HLLE, device=device, arithmetic=arith)
+        D.upload(h, hu, hv, b)
+        D.exchange_bathymetry()
+        D.step(steps)
+        D.sync()
+        states[name] = D.download()[0][m].astype(np.float64)
+        D.close()
+    R = oracle.Domain(geo["nx_cols"], geo["ny_rows"], geo["dx"], geo["dy"], outer=geo["boundary"], solver=oracle.HLLE,
+                      precision=64)
+    R.set_state(h, hu, hv, b)
+    R.bathymetry_ghosts()
+    R.step_parallel(steps)
+    h64 = R.get_state(np.float64)[0][m]
+    m0 = float(np.sum(h[m].astype(np.float64)))
+    out = {"workload": "tsunami 2048^2 as 4x4 blocks of 512^2, HLLE, unsplit, %d steps from the initial state" % steps,
+           "against": "FP64 oracle (CPU restatement of the reference's block code in double)", "steps": steps}
+    for name in ("fast", "exact"):
+        d = states[name] - h64
+        out[name] = {"rel_l1_h": float(np.abs(d).sum() / np.abs(h64).sum()), "max_abs_dh": float(np.abs(d).max()),
+                     "mass_drift_rel": float(abs(states[name].sum() - m0) / m0)}
+    out["exact"]["note"] = "bit-identical to the FP32 oracle (the reference's float arithmetic)"
+    out["fp64_mass_drift_rel"] = float(abs(h64.sum() - m0) / m0)
+    out["clamp_mass"] = 0.0
+    return out
 
 
 def cpu_baseline(seconds=12.0):
@@ -187,56 +274,181 @@ def dist_barrier(world):
         dist.barrier()
 
 
+def host_cpu():
+    """(cores usable, CPU model) of this host"""
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+    model = "unknown"
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                model = line.split(":", 1)[1].strip()
+                break
+    except Exception:
+        pass
+    return int(cores), model
+
+
+def reference_binary():
+    """The reference's stock overdecomposed driver (src/examples/swe_mpi_overdecomp.cpp
+    with its blocks, release flags and OpenMP), built from its sources on this
+    host by oracle/ref/Makefile; None where the sources are absent."""
+    import oracle
+    try:
+        if not oracle.reference_available():
+            oracle.stage_reference()
+        if oracle.reference_available():
+            return oracle.build_reference_perf()
+    except Exception as e:
+        log("reference build failed:", e)
+    return None
+
+
+def reference_run(binary, duration, blocks=N_BLOCKS, cells=N_CELLS_SIDE):
+    """One run of the stock driver at cells^2 over `blocks` blocks for
+    `duration` simulated seconds on every host core; returns (cell-updates,
+    wall seconds).  Cell-updates come from the driver's own log (FLOP_COUNT /
+    270, src/tools/Collector.hpp:129-142, 270 flop per cell-update at
+    src/blocks/SWE_DimensionalSplittingMpi.cpp:458).  Its WALL_TIME column is
+    not usable: the driver folds the blocks' collectors into its own with a
+    minimum over wall time (src/tools/Collector.hpp:42-43), and the blocks
+    never run that counter, so the log holds 0; the wall time is taken around
+    the process instead, and the set-up cost is removed by the caller."""
+    import tempfile
+    cores, _ = host_cpu()
+    with tempfile.TemporaryDirectory() as tmp:
+        base = os.path.join(tmp, "ref")
+        env = dict(os.environ, OMP_NUM_THREADS=str(cores))
+        t0 = time.perf_counter()
+        r = subprocess.run([binary, "-x", str(cells), "-y", str(cells), "-b", str(blocks), "-t", repr(float(duration)),
+                            "-n", "1", "-o", base, "-w", "0", "-l", "0"], capture_output=True, text=True, env=env,
+                           cwd=tmp)
+        el = time.perf_counter() - t0
+        if r.returncode != 0:
+            raise RuntimeError("reference driver failed: " + r.stderr[-500:])
+        rows = open(base + ".log").read().strip().splitlines()
+        flop = float(rows[-1].split(",")[1])
+    return flop / 270.0, el
+
+
 def run_reference(args, world, rank):
-    """The reference's algorithm on the host cores: the oracle (a line-by-line
-    restatement of the reference's block code, bit-identical to it where the
-    reference compiles) with one OpenMP thread per block, like the
-    overdecomposed driver.  One step = one full time step of the 2048^2 domain."""
+    """The reference's own CPU path on the host cores: its stock
+    overdecomposed driver (swe_benchmark_mpioverdecomp: 16 blocks of 512^2,
+    OpenMP over the blocks, HLLE -- the solver its build selects) timed as
+    built from its sources on this host.  Each step is one run over a short
+    simulated span; the cost of a run that only sets up and takes a few steps
+    is subtracted.  Without the sources, the oracle (a line-by-line
+    restatement of the reference's block code) on all host cores."""
     if rank != 0:
         return 0
-    import oracle
-    import swe_gb300 as swe
-    oracle.build()
-    geo, h, hu, hv, b = swe.init_domain(swe.SCENARIO_TSUNAMI, N_CELLS_SIDE, N_CELLS_SIDE, N_BLOCKS,
-                                        [N_CELLS_SIDE, SEED, 100000.0])
-    R = oracle.Domain(geo["nx_cols"], geo["ny_rows"], geo["dx"], geo["dy"], outer=geo["boundary"], solver=oracle.HLLE)
-    R.set_state(h, hu, hv, b)
-    R.bathymetry_ghosts()
-    threads = 1
-    for _ in range(max(args.warmup, 3)):
-        _, threads = R.step_parallel(1)
-    times = []
-    for _ in range(args.steps):
-        t0 = time.perf_counter()
-        R.step_parallel(1)
-        times.append(time.perf_counter() - t0)
-    cells = N_CELLS_SIDE * N_CELLS_SIDE
-    per = sum(times) / len(times)
-    value = cells / per
-    sample = "%d full time steps of the 2048^2 workload, oracle with OpenMP over 16 blocks on %d threads" % (
-        args.steps, threads)
+    cores, model = host_cpu()
+    binary = reference_binary()
+    if binary:
+        span = float(os.environ.get("SWE_REF_SPAN", "0.5"))
+        u0, w0 = reference_run(binary, 0.02)  # set-up and the first steps
+        for _ in range(max(args.warmup, 1) - 1):
+            reference_run(binary, 0.02)
+        rates, secs = [], []
+        for _ in range(args.steps):
+            u, w = reference_run(binary, span)
+            rates.append((u - u0) / max(w - w0, 1e-6))
+            secs.append(w - w0)
+        value = statistics.median(rates)
+        sample = ("%d runs of the stock swe_benchmark_mpioverdecomp -x %d -y %d -b %d -t %g (its radial-bathymetry dam "
+                  "break, HLLE), minus a -t 0.02 run's set-up; %d OpenMP threads on %s" % (
+                      args.steps, N_CELLS_SIDE, N_CELLS_SIDE, N_BLOCKS, span, cores, model))
+        kind = "reference"
+        ms_per_step = 1e3 * N_CELLS_SIDE * N_CELLS_SIDE / value
+    else:
+        import oracle
+        import swe_gb300 as swe
+        oracle.build()
+        geo, h, hu, hv, b = swe.init_domain(swe.SCENARIO_TSUNAMI, N_CELLS_SIDE, N_CELLS_SIDE, N_BLOCKS,
+                                            [N_CELLS_SIDE, SEED, 100000.0])
+        R = oracle.Domain(geo["nx_cols"], geo["ny_rows"], geo["dx"], geo["dy"], outer=geo["boundary"],
+                          solver=oracle.HLLE)
+        R.set_state(h, hu, hv, b)
+        R.bathymetry_ghosts()
+        threads = 1
+        for _ in range(max(args.warmup, 3)):
+            _, threads = R.step_parallel(1)
+        times = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            R.step_parallel(1)
+            times.append(time.perf_counter() - t0)
+        per = sum(times) / len(times)
+        value = N_CELLS_SIDE * N_CELLS_SIDE / per
+        ms_per_step = 1e3 * per
+        cores = int(threads)
+        kind = "port"
+        sample = "%d full time steps of the 2048^2 workload, oracle with OpenMP over 16 blocks on %d threads (%s)" % (
+            args.steps, threads, model)
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * per, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded tsunami scenario)",
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": workload_config({"parallelism": "host cores"}),
-            "cpu_baseline": {"value": value, "unit": "cell-updates/s", "cores": int(threads), "kind": "port",
-                             "sample": sample},
+            "cpu_baseline": {"value": value, "unit": "cell-updates/s", "cores": int(cores), "kind": kind,
+                             "sample": sample, "cpu_model": model},
             "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
 
 
-def lts_measure(swe, device, intervals=6):
+def lts_fp64_proxy(swe, device, n=256, duration=200.0):
+    """Error and mass of local time stepping against the FP64 oracle, on a
+    coarser copy of the benchmark's set-up (n^2 as 8x8 blocks, the same 50 km
+    shoreline ramp and bump, 1 s intervals, `duration` s): the FP64 oracle of
+    the 2048^2 run would take minutes on the host."""
+    import oracle
+    oracle.build()
+    geo, h, hu, hv, b = swe.init_domain(swe.SCENARIO_SHORELINE, n, n, 64, [SEED, 50000.0])
+    D = swe.Domain(geo["nx_cols"], geo["ny_rows"], geo["dx"], geo["dy"], boundary=geo["boundary"], solver=swe.HLLE,
+                   device=device, lts_max_timestep=1.0, duration=duration)
+    D.upload(h, hu, hv, b)
+    D.exchange_bathymetry()
+    D.lts_advance(duration)
+    g = D.download()[0].astype(np.float64)
+    D.close()
+    res = {}
+    for p in (32, 64):
+        R = oracle.Domain(geo["nx_cols"], geo["ny_rows"], geo["dx"], geo["dy"], outer=geo["boundary"], solver=oracle.HLLE,
+                          precision=p, lts_max_timestep=1.0, duration=duration)
+        R.set_state(h, hu, hv, b)
+        R.bathymetry_ghosts()
+        for _ in range(int(round(duration))):
+            R.lts_interval()
+        res[p] = (R.get_state(np.float64)[0], R.clamp_mass)
+    m = []
+    for k in range(64):
+        nx, ny = geo["nx_cols"][k // 8], geo["ny_rows"][k % 8]
+        a = np.zeros((nx + 2, ny + 2), bool)
+        a[1:-1, 1:-1] = True
+        m.append(a.ravel())
+    m = np.concatenate(m)
+    h64 = res[64][0][m]
+    m0 = float(np.sum(h[m].astype(np.float64)))
+    return {"workload": "%dx%d as 8x8 blocks, same ramp and bump, %g s" % (n, n, duration),
+            "rel_l1_h_gpu": float(np.abs(g[m] - h64).sum() / np.abs(h64).sum()),
+            "rel_l1_h_fp32_oracle": float(np.abs(res[32][0][m] - h64).sum() / np.abs(h64).sum()),
+            "max_abs_dh_gpu": float(np.abs(g[m] - h64).max()),
+            "mass_change_rel_gpu": float((g[m].sum() - m0) / m0),
+            "mass_change_rel_fp64": float((h64.sum() - m0) / m0),
+            "clamp_mass_rel_fp64": float(res[64][1] / m0),
+            "note": "outflow sides: mass change = outflow through the sides + depth the dry clamp added"}
+
+
+def lts_measure(swe, device, duration=200.0):
     """Local time stepping at 2048^2 as 8x8 blocks of 256^2 over a 50 km
     shoreline ramp (bathymetry -4000 m to +50 m across x, seeded Gaussian
     bump), HLLE, synchronisation intervals of 1 s: blocks step at 2^k
-    substeps per interval.  One warm-up interval, then `intervals` timed ones
-    (host clock around the device-driven interval loop); cell-updates summed
-    over the blocks' own steps."""
+    substeps per interval.  The first interval is the warm-up; the rest up to
+    `duration` s simulated are timed (host clock around the device-driven
+    interval loop); cell-updates summed over the blocks' own steps."""
     n, nb = 2048, 64
     geo, h, hu, hv, b = swe.init_domain(swe.SCENARIO_SHORELINE, n, n, nb, [SEED, 50000.0])
     D = swe.Domain(geo["nx_cols"], geo["ny_rows"], geo["dx"], geo["dy"], boundary=geo["boundary"], solver=swe.HLLE,
-                   device=device, lts_max_timestep=1.0, duration=200.0)
+                   device=device, lts_max_timestep=1.0, duration=duration)
     D.upload(h, hu, hv, b)
     D.exchange_bathymetry()
     D.lts_advance(1.0)
@@ -244,49 +456,82 @@ def lts_measure(swe, device, intervals=6):
                       for k in range(nb)], dtype=np.float64)
     s0 = D.block_steps()
     t0 = time.perf_counter()
-    done, t = D.lts_advance(1.0 + intervals)
+    done, t = D.lts_advance(duration)
     el = time.perf_counter() - t0
     s1 = D.block_steps()
     _, _, iters, per_interval = D.lts_state()
+    status = D.status()
     updates = float(np.dot(cells, (s1 - s0).astype(np.float64)))
     D.close()
     levels = sorted(set(int(v) for v in per_interval))
-    return {"workload": "local time stepping, shoreline ramp 2048x2048 as 8x8 blocks of 256^2, HLLE, 1 s intervals",
+    return {"workload": "local time stepping, shoreline ramp 2048x2048 as 8x8 blocks of 256^2, HLLE, 1 s intervals, "
+                        "%g s simulated" % duration,
             "value": updates / el, "unit": "cell-updates/s (sum over blocks of cells x own steps)",
-            "intervals": done, "seconds": el, "block_steps_per_interval": levels,
-            "mean_steps_per_block_interval": float(np.mean((s1 - s0) / max(1, done)))}
+            "intervals": done, "t_end": t, "seconds": el, "block_steps_per_interval": levels,
+            "mean_steps_per_block_interval": float(np.mean((s1 - s0) / max(1, done))), "device_status": status,
+            "fp64_proxy": lts_fp64_proxy(swe, device, duration=duration)}
 
 
 def ensemble_measure(swe, device, steps=100, count=256):
     """Batched ensemble: 256 independent radial dam breaks (nx, ny uniform in
     64, 96, ..., 1024; radius U(0.05, 0.3) L; inner height U(5, 20) m, outer
     U(1, 5) m; b = 0; one seed) in one handle, tile shape chosen by the tuner,
-    100 steps each at its own CFL dt, captured-graph replay (swe_gpu_advance).
-    Cell-updates summed over the instances."""
+    100 steps each at its own CFL dt, captured-graph replay (swe_gpu_advance),
+    in both arithmetics.  Cell-updates summed over the instances.  Accuracy:
+    the first 8 instances against the FP64 oracle after the same steps."""
     import torch
+    import oracle
     inst, states = swe.dam_break_ensemble(count, seed=SEED)
-    E = swe.Ensemble(inst, solver=swe.HLLE, device=device)
-    E.upload(*[np.concatenate([st[i] for st in states]) for i in range(4)])
-    E.exchange_bathymetry()
-    rows, cols, _ = E.autotune(trial_steps=3)
-    E.advance(1e30, max_steps=16)  # warm-up (graph capture)
-    stream = torch.cuda.Stream()
-    E.set_stream(stream.cuda_stream)
-    s0 = E.group_state()[2].astype(np.int64)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with torch.cuda.stream(stream):
-        e0.record(stream)
-        n, _ = E.advance(1e30, max_steps=steps)
-        e1.record(stream)
-        stream.synchronize()
-    ms = e0.elapsed_time(e1)
-    s1 = E.group_state()[2].astype(np.int64)
     cells = np.array([nx * ny for nx, ny, *_ in inst], dtype=np.float64)
-    updates = float(np.dot(cells, (s1 - s0).astype(np.float64)))
-    E.close()
-    return {"workload": "256 radial dam breaks, nx, ny in 64..1024, HLLE, unsplit, own dt each, graph replay",
-            "value": updates / (ms * 1e-3), "unit": "cell-updates/s (sum over instances)", "steps": int(n),
-            "cells": int(cells.sum()), "ms": ms, "tile_rows": rows, "tile_cols": cols}
+    out = {"workload": "256 radial dam breaks, nx, ny in 64..1024, HLLE, unsplit, own dt each, graph replay",
+           "unit": "cell-updates/s (sum over instances)", "cells": int(cells.sum())}
+    finals = {}
+    for name, arith in (("exact", swe.EXACT), ("fast", swe.FAST)):
+        E = swe.Ensemble(inst, solver=swe.HLLE, device=device, arithmetic=arith)
+        E.upload(*[np.concatenate([st[i] for st in states]) for i in range(4)])
+        E.exchange_bathymetry()
+        rows, cols, _ = E.autotune(trial_steps=3)
+        E.upload(*[np.concatenate([st[i] for st in states]) for i in range(4)])
+        E.advance(1e30, max_steps=16)  # warm-up (graph capture)
+        stream = torch.cuda.Stream()
+        E.set_stream(stream.cuda_stream)
+        s0 = E.group_state()[2].astype(np.int64)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            n, _ = E.advance(1e30, max_steps=steps)
+            e1.record(stream)
+            stream.synchronize()
+        ms = e0.elapsed_time(e1)
+        s1 = E.group_state()[2].astype(np.int64)
+        updates = float(np.dot(cells, (s1 - s0).astype(np.float64)))
+        finals[name] = (E.download()[0], int(s1[0]))
+        E.close()
+        out[name] = {"value": updates / (ms * 1e-3), "steps": int(n), "ms": ms, "tile_rows": rows, "tile_cols": cols}
+    out["value"] = max(out["exact"]["value"], out["fast"]["value"])
+    # accuracy of the first instances after the same number of steps (the
+    # warm-up's 16 plus the timed ones)
+    oracle.build()
+    errs = {"fast": [], "exact": []}
+    off = 0
+    for i in range(8):
+        nx, ny, dx, dy, bnd = inst[i]
+        sz = (nx + 2) * (ny + 2)
+        R = oracle.Domain([nx], [ny], dx, dy, outer=bnd, solver=oracle.HLLE, precision=64)
+        R.set_state(*states[i])
+        R.bathymetry_ghosts()
+        R.step(finals["fast"][1])
+        h64 = R.get_state(np.float64)[0]
+        a = np.zeros((nx + 2, ny + 2), bool)
+        a[1:-1, 1:-1] = True
+        a = a.ravel()
+        for name in ("fast", "exact"):
+            g = finals[name][0][off:off + sz].astype(np.float64)
+            errs[name].append(float(np.abs(g[a] - h64[a]).sum() / np.abs(h64[a]).sum()))
+        off += sz
+    out["fp64_first8"] = {"steps": finals["fast"][1], "rel_l1_h_fast_max": max(errs["fast"]),
+                          "rel_l1_h_exact_max": max(errs["exact"])}
+    return out
 
 
 def split_measure(swe, device, steps=20):
@@ -462,6 +707,27 @@ def profile_surrogate(n):
     return 0
 
 
+def cpu_reference_baseline(args):
+    """cpu_baseline of the gb300 line: the reference's stock driver on the
+    host cores (a bounded sample), else the oracle port"""
+    binary = reference_binary()
+    cores, model = host_cpu()
+    if binary:
+        span = float(os.environ.get("SWE_REF_SPAN", "0.5"))
+        u0, w0 = reference_run(binary, 0.02)
+        rates = []
+        for _ in range(3):
+            u, w = reference_run(binary, span)
+            rates.append((u - u0) / max(w - w0, 1e-6))
+        return {"value": statistics.median(rates), "unit": "cell-updates/s", "cores": cores, "kind": "reference",
+                "cpu_model": model,
+                "sample": "3 runs of the stock swe_benchmark_mpioverdecomp -x 2048 -y 2048 -b 16 -t %g (its radial-"
+                          "bathymetry dam break, HLLE) minus a -t 0.02 run's set-up, %d OpenMP threads" % (span, cores)}
+    base = cpu_baseline(float(os.environ.get("SWE_CPU_BASELINE_SECONDS", "12")))
+    base["cpu_model"] = model
+    return base
+
+
 def run_gb300(args, world, rank, local):
     import torch
     import swe_gb300 as swe
@@ -469,7 +735,11 @@ def run_gb300(args, world, rank, local):
     dev = torch.device("cuda", local)
     n = args.cells
     solvers = {"hlle": swe.HLLE, "fwave": swe.FWAVE, "augrie": swe.AUGRIE, "hybrid": swe.HYBRID}
-    D, geo, host = setup_domain(swe, local, n, solvers[args.profile_solver] if args.profile else swe.HLLE)
+    solver = solvers[args.profile_solver] if args.profile else swe.HLLE
+    # the headline path: fast arithmetic (one launch per step); --arith exact
+    # runs the bit-exact two-launch step instead
+    arith = swe.EXACT if args.arith == "exact" or solver in (swe.AUGRIE, swe.HYBRID) else swe.FAST
+    D, geo, host = setup_domain(swe, local, n, solver, arith)
     stream = torch.cuda.Stream(dev)  # a real stream handle: the library launches on it
     assert stream.cuda_stream != 0
     D.set_stream(stream.cuda_stream)
@@ -492,20 +762,12 @@ def run_gb300(args, world, rank, local):
 
         # timed region: exactly K steps, L2 flushed before each, CUDA events
         # around each step on the library's stream
-        starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-        ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
         stream.synchronize()
         dist_barrier(world)
         launches0 = D.launch_count()
-        for i in range(args.steps):
-            flush.zero_()
-            starts[i].record(stream)
-            D.step(1)
-            ends[i].record(stream)
-        stream.synchronize()
+        step_ms = timed_steps(D, stream, flush, args.steps)
         dist_barrier(world)
         launches = D.launch_count() - launches0
-    step_ms = [s_.elapsed_time(e) for s_, e in zip(starts, ends)]
     total_ms = dist_max(sum(step_ms), world)
     ms_per_step = total_ms / args.steps
     if args.profile:
@@ -514,22 +776,7 @@ def run_gb300(args, world, rank, local):
         D.close()
         return 0
 
-    # per-kernel breakdown: events between the three launches of each step
-    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
-    with torch.cuda.stream(stream):
-        for i in range(args.steps):
-            flush.zero_()
-            ev[i][0].record(stream)
-            D.set_ghost_layer()
-            ev[i][1].record(stream)
-            D.compute_fluxes()
-            ev[i][2].record(stream)
-            D.update_unknowns()
-            ev[i][3].record(stream)
-        stream.synchronize()
-    t_ghost = statistics.mean(e[0].elapsed_time(e[1]) for e in ev)
-    t_speed = statistics.mean(e[1].elapsed_time(e[2]) for e in ev)
-    t_update = statistics.mean(e[2].elapsed_time(e[3]) for e in ev)
+    kt = kernel_times(D, stream, flush, args.steps)
     status = D.status()
 
     # end to end through the C ABI on host buffers: upload h, hu, hv, b from
@@ -565,49 +812,78 @@ def run_gb300(args, world, rank, local):
     e2e_s = dist_max((time.perf_counter() - t0) / e2e_steps, world)
     h2d = sum(p.nbytes for p in pn)
     d2h = sum(o.nbytes for o in on)
+    D.close()
+
+    # the bit-exact step (identical to the reference's float arithmetic) on
+    # the same workload, for comparison
+    exact = None
+    if arith == swe.FAST:
+        E, _, _ = setup_domain(swe, local, n, solver, swe.EXACT)
+        E.set_stream(stream.cuda_stream)
+        with torch.cuda.stream(stream):
+            for _ in range(max(args.warmup, 3)):
+                flush.zero_()
+                E.step(1)
+        ems = timed_steps(E, stream, flush, args.steps)
+        ekt = kernel_times(E, stream, flush, args.steps)
+        E.close()
+        exact = {"ms_per_step": sum(ems) / len(ems), "value": cells / (1e-3 * sum(ems) / len(ems)),
+                 "unit": "cell-updates/s", "kernel_ms": ekt,
+                 "roofline_frac_update": BYTES_PER_CELL * cells / (ekt["update"] * 1e-3) / 1e9 / peaks()[0],
+                 "arithmetic": "IEEE division and square root, no contraction: bit-identical to the oracle"}
 
     hbm, peak_kind = peaks()
     algo_bytes = BYTES_PER_CELL * cells
-    achieved = algo_bytes / (t_update * 1e-3) / 1e9
+    t_kernel = kt["update"] + kt["speed"]  # fast: the one step kernel (compute_fluxes launches nothing)
+    achieved = algo_bytes / (t_kernel * 1e-3) / 1e9
     step_achieved = algo_bytes / (ms_per_step * 1e-3) / 1e9
     traffic, warp_inst = None, None
     try:
         with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
             prof = json.load(f)
-        traffic = prof.get("update_kernel_dram_bytes_per_launch")
-        warp_inst = prof.get("update_kernel_warp_instructions_per_launch")
+        key = "fast_kernel" if arith == swe.FAST else "update_kernel"
+        traffic = prof.get(key + "_dram_bytes_per_launch")
+        warp_inst = prof.get(key + "_warp_instructions_per_launch")
     except Exception:
         pass
     sms = torch.cuda.get_device_properties(dev).multi_processor_count
 
+    acc = accuracy_measure(swe, local) if rank == 0 else None
     lts = lts_measure(swe, local)
     ens = ensemble_measure(swe, local)
     sur = surrogate_measure(swe, local) if rank == 0 else None
     split = split_measure(swe, local) if rank == 0 else None
-    base = cpu_baseline(float(os.environ.get("SWE_CPU_BASELINE_SECONDS", "12"))) if rank == 0 else None
+    base = cpu_reference_baseline(args) if rank == 0 else None
     clocks = clk.summary()
     issue = None
     if warp_inst and clocks.get("sm_mhz"):
-        # the update pass is issue-bound: its warp instructions (ncu, one launch)
-        # per second against one instruction per SM sub-partition per cycle
+        # warp instructions of one launch (ncu) per second against one
+        # instruction per SM sub-partition per cycle
         issue_peak = sms * 4 * clocks["sm_mhz"] * 1e6
-        issue_achieved = warp_inst / (t_update * 1e-3)
+        issue_achieved = warp_inst / (t_kernel * 1e-3)
         issue = {"warp_instructions_per_launch": warp_inst, "achieved": issue_achieved, "peak": issue_peak,
                  "unit": "warp instructions/s", "frac": issue_achieved / issue_peak,
                  "peak_from": "%d SMs x 4 sub-partitions x %.0f MHz (median SM clock under load)" % (sms, clocks["sm_mhz"])}
     if rank == 0:
+        kname = "fastStepKernel<HLLE> (one launch per step)" if arith == swe.FAST else "sweepKernel<HLLE,unsplit,update>"
         line = {
             "metric": METRIC, "value": world * cells / (ms_per_step * 1e-3), "unit": "cell-updates/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded tsunami scenario, shapes of the 2048^2 benchmark)",
-            "config": workload_config({"parallelism": "replicas x%d" % world if world > 1 else "1 GPU"}),
-            "roofline": {"bound": "hbm", "kernel": "sweepKernel<HLLE,unsplit,update>", "achieved": achieved,
+            "config": workload_config({"parallelism": "replicas x%d" % world if world > 1 else "1 GPU",
+                                       "arithmetic": "fast (approximate rcp/rsqrt/sqrt, FMA; results equal to the "
+                                                     "reference to FP32 round-off, see accuracy)"
+                                       if arith == swe.FAST else "exact (bit-identical to the reference's float "
+                                                                 "arithmetic)"}),
+            "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved,
                          "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "peak_kind": peak_kind,
                          "traffic": traffic, "algorithmic_bytes_per_launch": algo_bytes,
                          "step_achieved": step_achieved, "step_frac": step_achieved / hbm, "issue": issue},
-            "kernel_ms": {"ghost": t_ghost, "speed": t_speed, "update": t_update},
-            "cpu_baseline": {k: base[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "kernel_ms": kt,
+            "exact": exact,
+            "accuracy": acc,
+            "cpu_baseline": {k: base[k] for k in ("value", "unit", "cores", "kind", "sample", "cpu_model")},
             "e2e": {"value": world * cells / e2e_s, "unit": "cell-updates/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "calls": "upload_async, step, download_async; sync at the end",
                     "synchronous_value": world * cells / e2e_sync_s},
@@ -615,7 +891,6 @@ def run_gb300(args, world, rank, local):
             "lts": lts, "ensemble": ens, "surrogate": sur, "split": split,
         }
         print(json.dumps(line), flush=True)
-    D.close()
     dist_barrier(world)
     return 0
 
@@ -626,6 +901,8 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--arith", default="fast", choices=["fast", "exact"],
+                    help="arithmetic of the timed step (fast: one launch per step, FP32 round-off; exact: bit-identical)")
     ap.add_argument("--cells", type=int, default=N_CELLS_SIDE, help="cells per side (profiling cases only)")
     ap.add_argument("--profile", action="store_true", help="timed steps only (for ncu captures)")
     ap.add_argument("--profile-solver", default="hlle", choices=["hlle", "fwave", "augrie", "hybrid"],

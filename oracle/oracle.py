@@ -22,7 +22,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 REF_DIR = os.path.join(HERE, "_ref")
-REFERENCE_SRC = "/root/reference"
+# the reference's source tree: SWE_REFERENCE_SRC, else the staged copy
+# (oracle/ref/stage.sh) under baseline/_ref
+REFERENCE_SRC = os.environ.get("SWE_REFERENCE_SRC") or os.path.join(os.path.dirname(HERE), "baseline", "_ref")
 
 # solver ids (same numbering as the product's C-ABI)
 FWAVE, AUGRIE, HYBRID, HLLE = 1, 2, 3, 4
@@ -66,6 +68,8 @@ def lib():
         L.oracle_domain_advance.argtypes = [C.c_void_p, C.c_double, C.c_int, C.c_void_p]
         L.oracle_domain_time.restype = C.c_double
         L.oracle_domain_time.argtypes = [C.c_void_p]
+        L.oracle_domain_clamp_mass.restype = C.c_double
+        L.oracle_domain_clamp_mass.argtypes = [C.c_void_p]
         L.oracle_domain_lts_interval.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
         L.oracle_domain_lts_iteration.argtypes = [C.c_void_p]
         L.oracle_domain_lts_blocks.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
@@ -151,6 +155,11 @@ class Domain:
     def time(self):
         return lib().oracle_domain_time(self.h)
 
+    @property
+    def clamp_mass(self):
+        """depth the dry clamp added so far (sum of -h over the cells it reset)"""
+        return lib().oracle_domain_clamp_mass(self.h)
+
     def lts_iteration(self):
         """one inner local-time-stepping iteration (interval end included when it completes one)"""
         return lib().oracle_domain_lts_iteration(self.h)
@@ -179,8 +188,23 @@ def reference_available():
     return os.path.isdir(os.path.join(REFERENCE_SRC, "src", "blocks"))
 
 
+def stage_reference():
+    """Copy the reference's source tree into baseline/_ref (oracle/ref/stage.sh,
+    which knows where the tree lies on the build machine); False where there
+    is none to copy."""
+    r = subprocess.run(["sh", os.path.join(HERE, "ref", "stage.sh")], capture_output=True, text=True)
+    return r.returncode == 0
+
+
 def build_reference():
     subprocess.run(["make", "-s", "-C", os.path.join(HERE, "ref"), "REF=" + REFERENCE_SRC], check=True)
+
+
+def build_reference_perf():
+    """The reference's stock overdecomposed driver with its release flags and
+    OpenMP (oracle/_ref/perf/swe_benchmark_mpioverdecomp): the CPU baseline."""
+    subprocess.run(["make", "-s", "-C", os.path.join(HERE, "ref"), "REF=" + REFERENCE_SRC, "perf"], check=True)
+    return os.path.join(REF_DIR, "perf", "swe_benchmark_mpioverdecomp")
 
 
 def ref_lib(macro):

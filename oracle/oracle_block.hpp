@@ -74,6 +74,7 @@ template <typename T> struct Block {
     int boundaryType[4] = {PASSIVE, PASSIVE, PASSIVE, PASSIVE};
     int neighbour[4] = {-1, -1, -1, -1};
     T maxTimestep = T(0);
+    double clampMass = 0.0;  // depth the dry clamp added (sum of -h over clamped cells), test bookkeeping
 
     // LTS state (src/blocks/SWE_Block.hh:214-229)
     bool localTimestepping = false;
@@ -207,6 +208,7 @@ template <typename T> struct Block {
                 hu(i, j) -= dt / dx * (huNR(i - 1, j - 1) + huNL(i, j - 1));
                 hv(i, j) -= dt / dy * (hvNA(i - 1, j - 1) + hvNB(i - 1, j));
                 if (h(i, j) < T(0)) {
+                    clampMass -= double(h(i, j));
                     h(i, j) = hu(i, j) = hv(i, j) = T(0);
                 } else if (double(h(i, j)) < 0.1) {
                     hu(i, j) = hv(i, j) = T(0);

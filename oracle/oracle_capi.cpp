@@ -229,6 +229,18 @@ int oracle_domain_advance(void *h, double target, int maxSteps, double *dts) {
 
 double oracle_domain_time(void *h) { return static_cast<Handle *>(h)->t; }
 
+/// depth the dry clamp of updateUnknowns (src/blocks/SWE_DimensionalSplittingMpi.cpp:502-515)
+/// has added over all blocks and steps: the sum of -h over cells it set from h < 0 to 0
+double oracle_domain_clamp_mass(void *h) {
+    auto *H = static_cast<Handle *>(h);
+    double m = 0.0;
+    if (H->f)
+        for (auto &B : H->f->blocks) m += B.clampMass;
+    else
+        for (auto &B : H->d->blocks) m += B.clampMass;
+    return m;
+}
+
 /// one local-time-stepping interval; blockSteps receives each block's step count
 int oracle_domain_lts_interval(void *h, int maxIterations, int *blockSteps) {
     auto *H = static_cast<Handle *>(h);

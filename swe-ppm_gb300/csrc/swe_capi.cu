@@ -632,7 +632,9 @@ bool buildFastPlan(swe_gpu_domain *D) {
     D->ctaSegF.clear();
     D->pieces.clear();
     D->arrF.clear();
-    const int TY = std::max(64, D->tileRows);
+    // whole warps of fastRows() rows per thread
+    const int rowsPerWarp = 32 * fast::fastRows();
+    const int TY = std::min(kMaxTileRows, (std::max(rowsPerWarp, D->tileRows) + rowsPerWarp - 1) / rowsPerWarp * rowsPerWarp);
     D->tileRowsF = TY;
     int sms = 148;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, D->device);

@@ -27,7 +27,6 @@
 //    last CTA turns the maximum into the next maxTimestep (:448-456), so a
 //    step is this one kernel: no speed pass.
 #include <cfloat>
-#include <cstdlib>
 
 #include "swe_fast.hpp"
 #include "swe_launch.hpp"
@@ -821,51 +820,33 @@ __global__ void __launch_bounds__(kMaxTileRows / R, MINB) fastStepKernel(const F
     }
 }
 
-// experiment selector (rows per thread, min CTAs per SM)
-static int variantSel() {
-    static int v = -1;
-    if (v < 0) {
-        const char *e = getenv("SWE_FAST_VARIANT");
-        v = e ? atoi(e) : 0;
-    }
-    return v;
-}
-template <int S> static void *kern(int v) {
-    switch (v) {
-    case 1: return (void *)fastStepKernel<S, 2, 5>;
-    case 2: return (void *)fastStepKernel<S, 4, 6>;
-    case 3: return (void *)fastStepKernel<S, 4, 5>;
-    case 5: return (void *)fastStepKernel<S, 4, 4>;
-    default: return (void *)fastStepKernel<S, 2, 4>;
-    }
-}
-int fastRows() { const int v = variantSel(); return (v == 2 || v == 3 || v == 5) ? 4 : 2; }
+/// rows per thread of the step kernel and its resident CTAs per SM (two
+/// rows: the second row's edges give each thread two independent chains;
+/// four CTAs of 128 threads keep the loop free of spills)
+constexpr int kRows = 2;
+constexpr int kMinCtas = 4;
+
+int fastRows() { return kRows; }
 
 cudaError_t launchFastStep(const FastDev &f, int solver, int grid, int tileRows, cudaStream_t s) {
-    const int threads = tileRows / fastRows();
-    void *k = solver == SOLVER_FWAVE ? kern<SOLVER_FWAVE>(variantSel()) : kern<SOLVER_HLLE>(variantSel());
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(grid);
-    cfg.blockDim = dim3(threads);
-    cfg.dynamicSmemBytes = kRingBytes;
-    cfg.stream = s;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    at[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    FastDev ff = f;
-    void *args[] = {&ff};
-    cudaError_t e = cudaLaunchKernelExC(&cfg, k, args);
+    const int threads = tileRows / kRows;
+    const cudaError_t e =
+        solver == SOLVER_FWAVE
+            ? launchPdlSmem(fastStepKernel<SOLVER_FWAVE, kRows, kMinCtas>, dim3(grid), dim3(threads), kRingBytes, s, f)
+            : launchPdlSmem(fastStepKernel<SOLVER_HLLE, kRows, kMinCtas>, dim3(grid), dim3(threads), kRingBytes, s, f);
     if (e != cudaSuccess) return e;
     return cudaGetLastError();
 }
 
 int fastOccupancy(int solver, int tileRows) {
     int a = 0;
-    const int threads = tileRows / fastRows();
-    void *k = solver == SOLVER_FWAVE ? kern<SOLVER_FWAVE>(variantSel()) : kern<SOLVER_HLLE>(variantSel());
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k, threads, kRingBytes);
+    const int threads = tileRows / kRows;
+    if (solver == SOLVER_FWAVE)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, fastStepKernel<SOLVER_FWAVE, kRows, kMinCtas>, threads,
+                                                      kRingBytes);
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, fastStepKernel<SOLVER_HLLE, kRows, kMinCtas>, threads,
+                                                      kRingBytes);
     return a;
 }
 
