@@ -231,6 +231,13 @@ int swe_gpu_lts_state(swe_gpu_domain *dom, float *t, int *intervals, int *iterat
  * sync, 4 next), stepSize, stepSizeCounter, timestepCounter, last-timestep
  * notice; border[4k..4k+3] = the neighbours' local times of the layers. */
 int swe_gpu_lts_blocks(swe_gpu_domain *dom, int *ints, float *border);
+/* getRoundTimestep (src/blocks/SWE_Block.hh:536-555) as the device applies it
+ * at the start of an interval: for each of the n time steps t (host array),
+ * the step size (power-of-two divisor of max_timestep_local, at most
+ * max_divisor) a block with that maxTimestep takes.  Evaluated on `device`;
+ * for tests and tools. */
+int swe_gpu_lts_round_timesteps(const float *t, int n, float max_timestep_local, int max_divisor, int *step_sizes,
+                                int device);
 /* dt groups (1 for a grid of blocks, one per instance of an ensemble or per
  * block under local time stepping) and their clocks: time, last dt and steps
  * (arrays of group-count entries, any may be null).  Synchronises. */
@@ -301,7 +308,8 @@ int swe_gpu_solve_edges(int solver, long long n, const float *hL, const float *h
  * block may need at most 4096 work units, ceil(ny/256) * ceil(nx/32); larger
  * blocks are rejected with SWE_GPU_ERR_INVALID.  The first call on a device
  * looks the array's device address up (cudaGetSymbolAddress); make that first
- * call before any stream capture.  Every call on a device shares the array and
+ * call before any stream capture.  A call that meets a CUDA error forgets the
+ * address, so the next call looks it up again (after a cudaDeviceReset).  Every call on a device shares the array and
  * clears it when it starts: calls that overlap on the GPU race. */
 int swe_gpu_step_block_noalloc(int solver, int semantics, int nx, int ny, float dx, float dy, const int *boundary4,
                                int ld, float *h, float *hu, float *hv, const float *b, float *h_out, float *hu_out,

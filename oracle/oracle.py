@@ -68,6 +68,8 @@ def lib():
         L.oracle_domain_advance.argtypes = [C.c_void_p, C.c_double, C.c_int, C.c_void_p]
         L.oracle_domain_time.restype = C.c_double
         L.oracle_domain_time.argtypes = [C.c_void_p]
+        L.oracle_lts_round_timesteps.argtypes = [_f32p, C.c_int, C.c_float, C.c_int,
+                                                 np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")]
         L.oracle_domain_clamp_mass.restype = C.c_double
         L.oracle_domain_clamp_mass.argtypes = [C.c_void_p]
         L.oracle_domain_lts_interval.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
@@ -176,6 +178,14 @@ class Domain:
         steps = np.zeros(self.bx * self.by, dtype=np.int32)
         it = lib().oracle_domain_lts_interval(self.h, int(max_iterations), _ptr(steps))
         return it, steps
+
+
+def lts_round_timesteps(t, max_timestep_local=1.0, max_divisor=1024):
+    """getRoundTimestep's step size for each time step in t (src/blocks/SWE_Block.hh:536-555)"""
+    t = np.ascontiguousarray(t, dtype=np.float32)
+    out = np.zeros(t.size, dtype=np.int32)
+    lib().oracle_lts_round_timesteps(t, t.size, float(max_timestep_local), int(max_divisor), out)
+    return out
 
 
 # ---------------------------------------------------------------------------

@@ -229,6 +229,20 @@ int oracle_domain_advance(void *h, double target, int maxSteps, double *dts) {
 
 double oracle_domain_time(void *h) { return static_cast<Handle *>(h)->t; }
 
+/// getRoundTimestep (src/blocks/SWE_Block.hh:536-555) of a block at the start
+/// of an interval, for every entry of t: the step sizes it picks
+int oracle_lts_round_timesteps(const float *t, int n, float tsync, int maxDivisor, int *stepSizes) {
+    for (int i = 0; i < n; i++) {
+        Block<float> B(1, 1, 1.f, 1.f);
+        B.maxTimestepLocal = tsync;
+        B.maxDivisor = maxDivisor;
+        B.stepSizeCounter = 0;
+        B.getRoundTimestep(t[i]);
+        stepSizes[i] = B.stepSize;
+    }
+    return 0;
+}
+
 /// depth the dry clamp of updateUnknowns (src/blocks/SWE_DimensionalSplittingMpi.cpp:502-515)
 /// has added over all blocks and steps: the sum of -h over cells it set from h < 0 to 0
 double oracle_domain_clamp_mass(void *h) {

@@ -1798,6 +1798,25 @@ int swe_gpu_speed_pass_stats(swe_gpu_domain *dom, int *tiles, int *evaluated) {
     return SWE_GPU_OK;
 }
 
+int swe_gpu_lts_round_timesteps(const float *t, int n, float max_timestep_local, int max_divisor, int *step_sizes,
+                                int device) {
+    if (n < 0 || (n > 0 && (!t || !step_sizes)) || !(max_timestep_local > 0.f) || max_divisor < 1)
+        return fail(SWE_GPU_ERR_INVALID, "bad argument");
+    if (n == 0) return SWE_GPU_OK;
+    CUDA_TRY(cudaSetDevice(device));
+    float *dt = nullptr;
+    int *ds = nullptr;
+    cudaError_t e = cudaMalloc(&dt, sizeof(float) * size_t(n));
+    if (e == cudaSuccess) e = cudaMalloc(&ds, sizeof(int) * size_t(n));
+    if (e == cudaSuccess) e = cudaMemcpy(dt, t, sizeof(float) * size_t(n), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = launchLtsRound(dt, n, max_timestep_local, max_divisor, ds, nullptr);
+    if (e == cudaSuccess) e = cudaMemcpy(step_sizes, ds, sizeof(int) * size_t(n), cudaMemcpyDeviceToHost);
+    cudaFree(dt);
+    cudaFree(ds);
+    if (e != cudaSuccess) return fail(SWE_GPU_ERR_CUDA, "lts rounding: %s", cudaGetErrorString(e));
+    return SWE_GPU_OK;
+}
+
 int swe_gpu_fast_pieces(const swe_gpu_domain *dom, int *out, int cap, int *count) {
     if (!dom || !count || cap < 0 || (cap > 0 && !out)) return fail(SWE_GPU_ERR_INVALID, "bad argument");
     if (!dom->fast) return fail(SWE_GPU_ERR_INVALID, "not a fast-arithmetic domain");
@@ -2138,17 +2157,27 @@ extern "C" int swe_gpu_step_block_noalloc(int solver, int semantics, int nx, int
     d.variant = VARIANT_TILE;  // one work unit per CTA, built by the set-up kernel
     cudaStream_t s = static_cast<cudaStream_t>(stream);
 
+    // any CUDA error drops the device's cached scratch address, so a call
+    // after the context was torn down (cudaDeviceReset) looks it up again
+    // instead of handing the kernels a stale pointer
+    auto check = [&](cudaError_t e, const char *what) {
+        if (e == cudaSuccess) return SWE_GPU_OK;
+        std::lock_guard<std::mutex> lock(g_noallocMutex);
+        g_noallocPtr[device] = nullptr;
+        return fail(SWE_GPU_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+    };
     noallocSetupKernel<<<(unsigned)std::max<long long>(1, std::min<long long>(64, (nunits + 255) / 256)), 256, 0, s>>>(
         scr, B, tileRows, tileCols, int(nunits));
-    CUDA_TRY(cudaGetLastError());
+    if ((rc = check(cudaGetLastError(), "set-up kernel"))) return rc;
     const int threads = 128;
     ghostKernel<<<dim3((2 * nx + 2 * ny + 4 + threads - 1) / threads, 1), threads, 0, s>>>(d, 0);
-    CUDA_TRY(cudaGetLastError());
-    CUDA_TRY(launchSpeed(d, int(nunits), tileRows, s));
-    CUDA_TRY(launchUpdate(d, int(nunits), tileRows, s));
+    if ((rc = check(cudaGetLastError(), "ghost kernel"))) return rc;
+    if ((rc = check(launchSpeed(d, int(nunits), tileRows, s), "speed pass"))) return rc;
+    if ((rc = check(launchUpdate(d, int(nunits), tileRows, s), "update pass"))) return rc;
     if (dt_out) {
-        CUDA_TRY(cudaMemcpyAsync(dt_out, &scr->group.dt, sizeof(float), cudaMemcpyDeviceToHost, s));
-        CUDA_TRY(cudaStreamSynchronize(s));
+        if ((rc = check(cudaMemcpyAsync(dt_out, &scr->group.dt, sizeof(float), cudaMemcpyDeviceToHost, s), "dt copy")))
+            return rc;
+        if ((rc = check(cudaStreamSynchronize(s), "stream synchronize"))) return rc;
     }
     return SWE_GPU_OK;
 }

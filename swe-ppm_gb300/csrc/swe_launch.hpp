@@ -60,6 +60,8 @@ int occupancyBound(int solver);
 cudaError_t launchLtsExchange(const DomainDev &d, int maxPerimeter, cudaStream_t s);
 cudaError_t launchLtsCheck(const DomainDev &d, cudaStream_t s);
 cudaError_t launchLtsDone(const DomainDev &d, cudaStream_t s);
+// getRoundTimestep of the speed pass for a device array of time steps
+cudaError_t launchLtsRound(const float *t, int n, float tsync, int maxDivisor, int *stepSize, cudaStream_t s);
 
 // resident CTAs per SM of the step kernels (the smaller of the two passes)
 int occupancyFH(int variant, int solver, int sem, bool update, int threads);

@@ -240,4 +240,23 @@ cudaError_t launchLtsDone(const DomainDev &d, cudaStream_t s) {
     return launchPdl(ltsDoneKernel, dim3(1), dim3(256), s, d);
 }
 
+/// getRoundTimestep of a block at the start of an interval for every entry
+/// of `t` (the step sizes it picks), as the speed pass computes it
+__global__ void ltsRoundKernel(const float *t, int n, float tsync, int maxDivisor, int *stepSize) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    LtsBlock L{};
+    LtsControl C{};
+    C.maxTimestepLocal = tsync;
+    C.maxDivisor = maxDivisor;
+    L.stepSizeCounter = 0;
+    ltsRoundTimestep(L, C, t[i]);
+    stepSize[i] = L.stepSize;
+}
+
+cudaError_t launchLtsRound(const float *t, int n, float tsync, int maxDivisor, int *stepSize, cudaStream_t s) {
+    ltsRoundKernel<<<(n + 255) / 256, 256, 0, s>>>(t, n, tsync, maxDivisor, stepSize);
+    return cudaGetLastError();
+}
+
 } // namespace swegb

@@ -45,7 +45,7 @@ EXPORTED = [
     "swe_gpu_snapshot_slabs_async", "swe_gpu_snapshot_wait", "swe_gpu_alloc_pinned", "swe_gpu_free_pinned",
     "swe_gpu_launch_count", "swe_gpu_speed_pass_stats", "swe_gpu_lts_advance", "swe_gpu_lts_state", "swe_gpu_lts_blocks",
     "swe_gpu_block_steps", "swe_gpu_ensemble_create", "swe_gpu_group_count", "swe_gpu_group_state",
-    "swe_gpu_retile", "swe_gpu_autotune", "swe_gpu_fast_pieces",
+    "swe_gpu_retile", "swe_gpu_autotune", "swe_gpu_fast_pieces", "swe_gpu_lts_round_timesteps",
     "swe_mlp_last_error", "swe_mlp_gemm_check", "swe_mlp_param_count", "swe_mlp_create", "swe_mlp_destroy",
     "swe_mlp_get_params", "swe_mlp_set_params", "swe_mlp_forward", "swe_mlp_solve", "swe_mlp_loss_grad",
     "swe_mlp_train", "swe_gpu_surrogate_step", "swe_gpu_surrogate_edge_count", "swe_gpu_log_edges",
@@ -113,6 +113,7 @@ def lib():
         L.swe_gpu_launch_count.argtypes = [vp, C.POINTER(C.c_longlong)]
         L.swe_gpu_speed_pass_stats.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int)]
         L.swe_gpu_fast_pieces.argtypes = [vp, C.c_void_p, C.c_int, C.POINTER(C.c_int)]
+        L.swe_gpu_lts_round_timesteps.argtypes = [vp, C.c_int, C.c_float, C.c_int, vp, C.c_int]
         L.swe_gpu_lts_advance.argtypes = [vp, C.c_float, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_float)]
         L.swe_gpu_lts_state.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_int), C.POINTER(C.c_int), vp]
         L.swe_gpu_lts_blocks.argtypes = [vp, vp, vp]
@@ -630,6 +631,15 @@ def dam_break_ensemble(count, seed, sizes=None, length=1000.0):
                                  [length, radius, hin, hout, 0.0, 0.0, 0.0]))
         inst.append((nx, ny, dx, dy, bnd))
     return inst, states
+
+
+def lts_round_timesteps(t, max_timestep_local=1.0, max_divisor=1024, device=0):
+    """the device's getRoundTimestep step size for each time step in t"""
+    t = np.ascontiguousarray(t, dtype=np.float32)
+    out = np.zeros(t.size, dtype=np.int32)
+    _check(lib().swe_gpu_lts_round_timesteps(_p(t), t.size, float(max_timestep_local), int(max_divisor), _p(out),
+                                             int(device)))
+    return out
 
 
 def solve_edges_device(solver, ptrs_in, ptrs_out, n, stream=None):

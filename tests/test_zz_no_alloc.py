@@ -20,6 +20,8 @@ torch = pytest.importorskip("torch")
     (4, 0, 1, [], 300, 260),                                  # HLLE, unsplit, ragged tiles
     (2, 0, 12, [3, 50000.0], 96, 64),                          # augmented solver, wet/dry shoreline
     (3, 1, 10, [1000.0, 100.0, 15.0, 10.0, 0.0], 128, 128),   # hybrid, split step
+    (1, 0, 10, [1000.0, 120.0, 12.0, 6.0, 0.0], 150, 90),     # f-wave, unsplit
+    (4, 1, 10, [1000.0, 150.0, 14.0, 7.0, 0.0], 200, 300),    # HLLE, split step over two row tiles
 ])
 def test_noalloc_step_matches_domain_step(swe, solver, semantics, scenario, params, nx, ny):
     geo, h, hu, hv, b = swe.init_domain(scenario, nx, ny, 1, params)
