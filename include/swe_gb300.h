@@ -88,9 +88,9 @@ typedef struct swe_gpu_desc {
     int tile_rows;       /* rows per CTA (multiple of 32, <= 256); 0 = default */
     int tile_cols;       /* max columns per work segment (<= 128 for the tile mapping); 0 = default */
     int device;          /* CUDA device ordinal */
-    int kernel_variant;  /* thread mapping of the sweep kernels: 0 = CTA tiles of
-                            tile_rows rows (default), 1 / 2 / 3 = warp strips of
-                            4 / 2 / 1 rows per lane */
+    int kernel_variant;  /* reserved, must be 0 (the sweep kernels' one thread
+                            mapping: CTA tiles of tile_rows rows); any other
+                            value is SWE_GPU_ERR_INVALID */
     int speed_pass;      /* 0 = bounded speed pass where available (f-wave or HLLE,
                             unsplit step, CTA tiles): exact wave speeds only where
                             the previous update's speed bounds can reach the
@@ -131,7 +131,7 @@ typedef struct swe_gpu_instance {
  * persistent launches (swe_gpu_step, swe_gpu_advance; graph replay).  Block k
  * is instance k for uploads, downloads and snapshots.  From `options` only
  * solver, semantics, split_dt_mode, tile_rows, tile_cols, device,
- * kernel_variant, speed_pass and arithmetic are used.  The reference runs independent
+ * kernel_variant (0), speed_pass and arithmetic are used.  The reference runs independent
  * scenarios as separate processes; this has no counterpart there. */
 int swe_gpu_ensemble_create(const swe_gpu_instance *instances, int count, const swe_gpu_desc *options,
                             swe_gpu_domain **out);

@@ -235,7 +235,6 @@ struct swe_gpu_domain {
     cudaStream_t stream = nullptr;     // stream launches go to
     cudaStream_t ownStream = nullptr;  // the handle's own stream
     int solver = SOLVER_HLLE, semantics = SEM_UNSPLIT, splitDtMode = SPLIT_DT_MAX;
-    int variant = VARIANT_WARP;
     int tileRows = 256, tileCols = 32;
     int tileColsArg = 0;              // segment-length cap asked for (0: default)
     std::vector<BlockDesc> blocks;
@@ -551,15 +550,10 @@ struct BlockSpec {
 };
 
 struct DomainOptions {
-    int device, solver, semantics, splitDtMode, variant, tileRows, tileCols, speedPass, arithmetic;
+    int device, solver, semantics, splitDtMode, tileRows, tileCols, speedPass, arithmetic;
     float ltsMaxTimestep, duration;
     int ngroups;
 };
-
-int variantOf(int kernelVariant) {
-    return kernelVariant == 1 ? VARIANT_WARP : kernelVariant == 2 ? VARIANT_WARP2 : kernelVariant == 3 ? VARIANT_WARP1
-                                                                                                       : VARIANT_TILE;
-}
 
 /// Balanced persistent partitions of both passes for the domain's current
 /// tile shape; tileColsArg > 0 caps the segment length.
@@ -570,27 +564,23 @@ void buildPartitions(swe_gpu_domain *D, int tileColsArg) {
     D->ctaSegU.clear();
     // Balanced persistent partitions, one per pass (the two kernels differ in
     // registers and therefore in resident CTAs): the (row tile, column) pairs
-    // of all blocks in order, split into `workers` equal runs (a worker is a
-    // CTA for the tile mapping, a warp for the warp mappings); a run that
-    // crosses a tile or a block boundary becomes several segments.  tile_cols,
+    // of all blocks in order, split into `workers` equal runs, one per CTA; a
+    // run that crosses a tile or a block boundary becomes several segments.  tile_cols,
     // when given, caps the segment length and raises the number of workers.
     for (int pass = 0; pass < 2; pass++) {
         int sms = 148;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, D->device);
-        const bool warp = D->variant != VARIANT_TILE;
-        const int rows = D->variant == VARIANT_WARP ? 4 : D->variant == VARIANT_WARP2 ? 2 : 1;
-        const int rowsPerTile = warp ? 32 * rows : D->tileRows;
-        const int occ = passOccupancy(D->variant, D->solver, D->semantics, pass == 1, D->tileRows);
-        const long long perSM = warp ? std::max(1, std::min(64, 4 * occ)) : std::max(1, std::min(16, occ));
+        const int rowsPerTile = D->tileRows;
+        const int occ = passOccupancy(D->solver, D->semantics, pass == 1, D->tileRows);
+        const long long perSM = std::max(1, std::min(16, occ));
         long long total = 0;
         for (const BlockDesc &B : D->blocks) total += (long long)((B.ny + rowsPerTile - 1) / rowsPerTile) * B.nx;
         long long workers = (long long)sms * perSM;
         if (tileColsArg > 0) workers = std::max(workers, (total + tileColsArg - 1) / tileColsArg);
         workers = std::max(1LL, std::min(total, workers));
-        if (warp) workers = (workers + 3) / 4 * 4;  // whole CTAs of 4 warps
         std::vector<WorkUnit> &units = pass ? D->unitsU : D->units;
         std::vector<int> &ctaSeg = pass ? D->ctaSegU : D->ctaSeg;
-        (pass ? D->gridU : D->grid) = int(warp ? workers / 4 : workers);
+        (pass ? D->gridU : D->grid) = int(workers);
         ctaSeg.assign(1, 0);
         long long pos = 0;  // global (tile, column) index
         int k = 0, tile = 0, col = 1;
@@ -600,7 +590,7 @@ void buildPartitions(swe_gpu_domain *D, int tileColsArg) {
             while (pos < end) {
                 const BlockDesc &B = D->blocks[k];
                 const long long take = std::min<long long>(end - pos, (long long)(B.nx + 1 - col));
-                const int cap = tileColsArg > 0 ? tileColsArg : (warp ? (1 << 30) : kMaxTileCols);
+                const int cap = tileColsArg > 0 ? tileColsArg : kMaxTileCols;
                 const int len = int(std::min<long long>(take, cap));
                 units.push_back(WorkUnit{k, 1 + tile * rowsPerTile, col, col + len});
                 pos += len;
@@ -772,7 +762,6 @@ int buildDomain(const std::vector<BlockSpec> &spec, const DomainOptions &o, swe_
     D->solver = o.solver;
     D->semantics = o.semantics;
     D->splitDtMode = o.splitDtMode;
-    D->variant = o.variant;
     D->tileColsArg = o.tileCols;
     int maxNy = 0;
     for (const BlockSpec &b : spec) maxNy = std::max(maxNy, b.ny);
@@ -832,7 +821,7 @@ int buildDomain(const std::vector<BlockSpec> &spec, const DomainOptions &o, swe_
     // (not under local time stepping: with one dt group per block every block's
     // own maximum needs exact edges, so many tiles are candidates and the full
     // pass, one streaming read of every edge, is faster)
-    D->bounded = D->variant == VARIANT_TILE && D->semantics == SEM_UNSPLIT &&
+    D->bounded = D->semantics == SEM_UNSPLIT &&
                  (D->solver == SOLVER_FWAVE || D->solver == SOLVER_HLLE) && o.speedPass == 0 && smallBlocks &&
                  !D->lts && !D->fast;
     if (D->bounded) {
@@ -912,7 +901,7 @@ int buildDomain(const std::vector<BlockSpec> &spec, const DomainOptions &o, swe_
         for (int f = 0; f < 3 && ok; f++)
             ok = cudaMalloc(&D->dRing[f], sizeof(float) * std::max(1LL, D->ringElems)) == cudaSuccess;
     }
-    D->edgeBuffered = D->solver == SOLVER_AUGRIE && D->semantics == SEM_UNSPLIT && !D->lts && D->variant == VARIANT_TILE &&
+    D->edgeBuffered = D->solver == SOLVER_AUGRIE && D->semantics == SEM_UNSPLIT && !D->lts &&
                       o.speedPass == 0;
     if (D->edgeBuffered) {
         D->edgeTiles = mlp::buildEdgeTiles(D->blocks);
@@ -993,7 +982,6 @@ int buildDomain(const std::vector<BlockSpec> &spec, const DomainOptions &o, swe_
     D->dev.solver = D->solver;
     D->dev.semantics = D->semantics;
     D->dev.splitDtMode = D->splitDtMode;
-    D->dev.variant = D->variant;
     D->dev.tileRows = D->tileRows;
     D->dev.lts = D->dLts;
     D->dev.ltsCtl = D->dLtsCtl;
@@ -1026,7 +1014,7 @@ int checkCommon(int solver, int semantics, const int boundary[4]) {
     return SWE_GPU_OK;
 }
 
-int checkArithmetic(int arithmetic, int solver, int semantics, bool lts, int kernelVariant) {
+int checkArithmetic(int arithmetic, int solver, int semantics, bool lts) {
     if (arithmetic == SWE_ARITH_EXACT) return SWE_GPU_OK;
     if (arithmetic != SWE_ARITH_FAST) return fail(SWE_GPU_ERR_INVALID, "unknown arithmetic %d", arithmetic);
     if (solver != SWE_SOLVER_FWAVE && solver != SWE_SOLVER_HLLE)
@@ -1034,7 +1022,13 @@ int checkArithmetic(int arithmetic, int solver, int semantics, bool lts, int ker
     if (semantics != SWE_SEMANTICS_UNSPLIT)
         return fail(SWE_GPU_ERR_INVALID, "fast arithmetic is offered for the unsplit step");
     if (lts) return fail(SWE_GPU_ERR_INVALID, "fast arithmetic is offered with global time stepping");
-    if (kernelVariant != 0) return fail(SWE_GPU_ERR_INVALID, "fast arithmetic uses the CTA-tile mapping (kernel_variant 0)");
+    return SWE_GPU_OK;
+}
+
+int checkVariant(int kernelVariant) {
+    if (kernelVariant != 0)
+        return fail(SWE_GPU_ERR_INVALID, "kernel_variant %d: the sweep kernels have one thread mapping (0, CTA tiles)",
+                    kernelVariant);
     return SWE_GPU_OK;
 }
 
@@ -1067,7 +1061,9 @@ int swe_gpu_domain_create(const swe_gpu_desc *desc, swe_gpu_domain **out) {
     rc = checkTiles(desc->tile_rows, desc->tile_cols);
     if (rc) return rc;
     const bool lts = desc->lts_max_timestep > 0.f;
-    rc = checkArithmetic(desc->arithmetic, desc->solver, desc->semantics, lts, desc->kernel_variant);
+    rc = checkArithmetic(desc->arithmetic, desc->solver, desc->semantics, lts);
+    if (rc) return rc;
+    rc = checkVariant(desc->kernel_variant);
     if (rc) return rc;
     std::vector<BlockSpec> spec;
     for (int k = 0; k < bx * by; k++) {
@@ -1091,7 +1087,6 @@ int swe_gpu_domain_create(const swe_gpu_desc *desc, swe_gpu_domain **out) {
     o.solver = desc->solver;
     o.semantics = desc->semantics;
     o.splitDtMode = desc->split_dt_mode;
-    o.variant = variantOf(desc->kernel_variant);
     o.tileRows = desc->tile_rows;
     o.tileCols = desc->tile_cols;
     o.speedPass = desc->speed_pass;
@@ -1110,7 +1105,9 @@ int swe_gpu_ensemble_create(const swe_gpu_instance *inst, int count, const swe_g
         return fail(SWE_GPU_ERR_INVALID, "ensembles step globally per instance (no local time stepping)");
     int rc = checkTiles(options->tile_rows, options->tile_cols);
     if (rc) return rc;
-    rc = checkArithmetic(options->arithmetic, options->solver, options->semantics, false, options->kernel_variant);
+    rc = checkArithmetic(options->arithmetic, options->solver, options->semantics, false);
+    if (rc) return rc;
+    rc = checkVariant(options->kernel_variant);
     if (rc) return rc;
     std::vector<BlockSpec> spec;
     for (int i = 0; i < count; i++) {
@@ -1138,7 +1135,6 @@ int swe_gpu_ensemble_create(const swe_gpu_instance *inst, int count, const swe_g
     o.solver = options->solver;
     o.semantics = options->semantics;
     o.splitDtMode = options->split_dt_mode;
-    o.variant = variantOf(options->kernel_variant);
     o.tileRows = options->tile_rows;
     o.tileCols = options->tile_cols;
     o.speedPass = options->speed_pass;
@@ -2154,7 +2150,6 @@ extern "C" int swe_gpu_step_block_noalloc(int solver, int semantics, int nx, int
     d.solver = solver;
     d.semantics = semantics;
     d.splitDtMode = SPLIT_DT_MAX;
-    d.variant = VARIANT_TILE;  // one work unit per CTA, built by the set-up kernel
     cudaStream_t s = static_cast<cudaStream_t>(stream);
 
     // any CUDA error drops the device's cached scratch address, so a call

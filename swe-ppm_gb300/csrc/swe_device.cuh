@@ -36,9 +36,6 @@ enum BoundaryType { OUTFLOW = 0, WALL = 1, INFLOW = 2, CONNECT = 3, CONNECT_WITH
 enum SplitDtMode { SPLIT_DT_MAX = 0, SPLIT_DT_LAST_EDGE = 1 };
 // states of a received ghost layer under local time stepping (src/blocks/SWE_Block.hh)
 enum GhostlayerState { GL_DONE = 0, GL_UNVALID = 1, GL_INTER = 2, GL_SYNC = 3, GL_NEXT = 4 };
-/// thread mapping of the sweep kernels: warp strips of 4, 2 or 1 rows per
-/// lane, or CTA tiles
-enum KernelVariant { VARIANT_WARP = 0, VARIANT_TILE = 1, VARIANT_WARP2 = 2, VARIANT_WARP1 = 3 };
 
 struct BlockDesc {
     int nx, ny;       // interior cells
@@ -151,7 +148,6 @@ struct DomainDev {
     GroupState *groups;
     int nblocks;
     int solver, semantics, splitDtMode;
-    int variant;             // KernelVariant
     int tileRows;            // TY of the CTA-tile mapping
     // bounded speed pass (null when the full speed pass is used), two
     // parities of ntiles entries each, parity p describing the state written

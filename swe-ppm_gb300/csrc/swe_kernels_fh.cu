@@ -1,51 +1,19 @@
 // Step kernels instantiated for the f-wave and HLLE solvers.
 #include "swe_launch.hpp"
 #include "swe_bound.cuh"
-#include "swe_warp.cuh"
+#include "swe_sweep.cuh"
 
 namespace swegb {
 
-
 template <int S> static cudaError_t speed(const DomainDev &d, int n, int th, cudaStream_t s) {
-    if (d.variant == VARIANT_WARP) {
-        if (d.semantics == SEM_SPLIT)
-            speedSplitWarpKernel<S, 4><<<n, 128, 0, s>>>(d);
-        else
-            sweepWarpKernel<S, SEM_UNSPLIT, false, 4><<<n, 128, 0, s>>>(d);
-    } else if (d.variant == VARIANT_WARP2) {
-        if (d.semantics == SEM_SPLIT)
-            speedSplitWarpKernel<S, 2><<<n, 128, 0, s>>>(d);
-        else
-            sweepWarpKernel<S, SEM_UNSPLIT, false, 2><<<n, 128, 0, s>>>(d);
-    } else if (d.variant == VARIANT_WARP1) {
-        if (d.semantics == SEM_SPLIT)
-            speedSplitWarpKernel<S, 1><<<n, 128, 0, s>>>(d);
-        else
-            sweepWarpKernel<S, SEM_UNSPLIT, false, 1><<<n, 128, 0, s>>>(d);
-    } else if (d.semantics == SEM_SPLIT) {
+    if (d.semantics == SEM_SPLIT)
         speedSplitKernel<S><<<n, th, 0, s>>>(d);
-    } else {
+    else
         sweepKernel<S, SEM_UNSPLIT, false><<<n, th, 0, s>>>(d);
-    }
     return cudaGetLastError();
 }
 template <int S> static cudaError_t update(const DomainDev &d, int n, int th, cudaStream_t s) {
-    if (d.variant == VARIANT_WARP) {
-        if (d.semantics == SEM_SPLIT)
-            sweepWarpKernel<S, SEM_SPLIT, true, 4><<<n, 128, 0, s>>>(d);
-        else
-            sweepWarpKernel<S, SEM_UNSPLIT, true, 4><<<n, 128, 0, s>>>(d);
-    } else if (d.variant == VARIANT_WARP2) {
-        if (d.semantics == SEM_SPLIT)
-            sweepWarpKernel<S, SEM_SPLIT, true, 2><<<n, 128, 0, s>>>(d);
-        else
-            sweepWarpKernel<S, SEM_UNSPLIT, true, 2><<<n, 128, 0, s>>>(d);
-    } else if (d.variant == VARIANT_WARP1) {
-        if (d.semantics == SEM_SPLIT)
-            sweepWarpKernel<S, SEM_SPLIT, true, 1><<<n, 128, 0, s>>>(d);
-        else
-            sweepWarpKernel<S, SEM_UNSPLIT, true, 1><<<n, 128, 0, s>>>(d);
-    } else if (d.semantics == SEM_SPLIT) {
+    if (d.semantics == SEM_SPLIT) {
         sweepKernel<S, SEM_SPLIT, true><<<n, th, 0, s>>>(d);
     } else {
         cudaError_t e = launchPdl(sweepKernel<S, SEM_UNSPLIT, true>, dim3(n), dim3(th), s, d);
@@ -75,24 +43,15 @@ template <class K> static int occ(K kernel, int th) {
 }
 
 /// resident CTAs per SM of one pass's kernel
-template <int S> static int occupancy(int variant, int sem, bool upd, int th) {
+template <int S> static int occupancy(int sem, bool upd, int th) {
     const bool split = sem == SEM_SPLIT;
-    if (variant == VARIANT_WARP)
-        return upd ? (split ? occ(sweepWarpKernel<S, SEM_SPLIT, true, 4>, 128) : occ(sweepWarpKernel<S, SEM_UNSPLIT, true, 4>, 128))
-                   : (split ? occ(speedSplitWarpKernel<S, 4>, 128) : occ(sweepWarpKernel<S, SEM_UNSPLIT, false, 4>, 128));
-    if (variant == VARIANT_WARP1)
-        return upd ? (split ? occ(sweepWarpKernel<S, SEM_SPLIT, true, 1>, 128) : occ(sweepWarpKernel<S, SEM_UNSPLIT, true, 1>, 128))
-                   : (split ? occ(speedSplitWarpKernel<S, 1>, 128) : occ(sweepWarpKernel<S, SEM_UNSPLIT, false, 1>, 128));
-    if (variant == VARIANT_WARP2)
-        return upd ? (split ? occ(sweepWarpKernel<S, SEM_SPLIT, true, 2>, 128) : occ(sweepWarpKernel<S, SEM_UNSPLIT, true, 2>, 128))
-                   : (split ? occ(speedSplitWarpKernel<S, 2>, 128) : occ(sweepWarpKernel<S, SEM_UNSPLIT, false, 2>, 128));
     return upd ? (split ? occ(sweepKernel<S, SEM_SPLIT, true>, th) : occ(sweepKernel<S, SEM_UNSPLIT, true>, th))
                : (split ? occ(speedSplitKernel<S>, th) : occ(sweepKernel<S, SEM_UNSPLIT, false>, th));
 }
 
-int occupancyFH(int variant, int solver, int sem, bool update, int threads) {
-    return solver == SOLVER_FWAVE ? occupancy<SOLVER_FWAVE>(variant, sem, update, threads)
-                           : occupancy<SOLVER_HLLE>(variant, sem, update, threads);
+int occupancyFH(int solver, int sem, bool update, int threads) {
+    return solver == SOLVER_FWAVE ? occupancy<SOLVER_FWAVE>(sem, update, threads)
+                                  : occupancy<SOLVER_HLLE>(sem, update, threads);
 }
 
 int occupancyBound(int solver) {

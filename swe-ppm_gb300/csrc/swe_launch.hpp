@@ -64,11 +64,11 @@ cudaError_t launchLtsDone(const DomainDev &d, cudaStream_t s);
 cudaError_t launchLtsRound(const float *t, int n, float tsync, int maxDivisor, int *stepSize, cudaStream_t s);
 
 // resident CTAs per SM of the step kernels (the smaller of the two passes)
-int occupancyFH(int variant, int solver, int sem, bool update, int threads);
-int occupancyAug(int variant, int solver, int sem, bool update, int threads);
-inline int passOccupancy(int variant, int solver, int sem, bool update, int threads) {
-    return (solver == SOLVER_FWAVE || solver == SOLVER_HLLE) ? occupancyFH(variant, solver, sem, update, threads)
-                                                           : occupancyAug(variant, solver, sem, update, threads);
+int occupancyFH(int solver, int sem, bool update, int threads);
+int occupancyAug(int solver, int sem, bool update, int threads);
+inline int passOccupancy(int solver, int sem, bool update, int threads) {
+    return (solver == SOLVER_FWAVE || solver == SOLVER_HLLE) ? occupancyFH(solver, sem, update, threads)
+                                                           : occupancyAug(solver, sem, update, threads);
 }
 
 inline cudaError_t launchSpeed(const DomainDev &d, int nunits, int threads, cudaStream_t s) {

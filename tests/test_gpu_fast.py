@@ -312,3 +312,6 @@ def test_fast_rejects_unsupported(swe):
     for kw in (dict(solver=2), dict(solver=3), dict(solver=4, semantics=1), dict(solver=4, lts_max_timestep=1.0)):
         with pytest.raises(swe.SweGpuError):
             swe.Domain(geo["nx_cols"], geo["ny_rows"], 1.0, 1.0, arithmetic=FAST, **kw)
+    for variant in (1, 2, 3):  # one thread mapping: a non-zero kernel_variant is refused
+        with pytest.raises(swe.SweGpuError):
+            swe.Domain(geo["nx_cols"], geo["ny_rows"], 1.0, 1.0, solver=4, kernel_variant=variant)

@@ -14,9 +14,9 @@ SOLVERS = {"hlle": 4, "fwave": 1, "augrie": 2, "hybrid": 3}
 
 
 def gpu_run(swe, cols, rows, dx, dy, outer, solver, h0, hu0, hv0, b0, nsteps, semantics=0, mode=0, tile_rows=0,
-            tile_cols=0, api="split", variant=0):
+            tile_cols=0, api="split"):
     D = swe.Domain(cols, rows, dx, dy, boundary=outer, solver=solver, semantics=semantics, split_dt_mode=mode,
-                   tile_rows=tile_rows, tile_cols=tile_cols, kernel_variant=variant)
+                   tile_rows=tile_rows, tile_cols=tile_cols)
     D.upload(h0, hu0, hv0, b0)
     D.exchange_bathymetry()
     dts = []
@@ -96,15 +96,13 @@ CASES = [
 ]
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2, 3])
 @pytest.mark.parametrize("solver", ["hlle", "fwave", "augrie", "hybrid"])
 @pytest.mark.parametrize("case", range(len(CASES)))
-def test_random_domains_unsplit(swe, oracle_mod, solver, case, variant):
+def test_random_domains_unsplit(swe, oracle_mod, solver, case):
     sid, params, nx, ny, nb, outer, tr, tc = CASES[case]
     geo, h0, hu0, hv0, b0 = swe.init_domain(sid, nx, ny, nb, params, boundary=outer)
     args = (geo["nx_cols"], geo["ny_rows"], geo["dx"], geo["dy"], outer, SOLVERS[solver], h0, hu0, hv0, b0, 8)
-    gpu, gdts = gpu_run(swe, *args, tile_rows=tr, tile_cols=tc, api="split" if case % 2 else "fused",
-                        variant=variant)
+    gpu, gdts = gpu_run(swe, *args, tile_rows=tr, tile_cols=tc, api="split" if case % 2 else "fused")
     ref, rdts = oracle_run(oracle_mod, *args)
     if case % 2:
         assert_bitwise(gdts, rdts.astype(np.float32), "dt")
@@ -142,16 +140,15 @@ def test_set_ghost_layer_after_update_equals_recomputed_ring(swe, solver, case):
         assert_bitwise(a, r, k)
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2, 3])
 @pytest.mark.parametrize("solver", ["hybrid", "hlle", "fwave", "augrie"])
 @pytest.mark.parametrize("mode", [0, 1])
 @pytest.mark.parametrize("shape", [(64, 64, 256, 32), (77, 301, 64, 5)])
-def test_split_semantics(swe, oracle_mod, solver, mode, shape, variant):
+def test_split_semantics(swe, oracle_mod, solver, mode, shape):
     nx, ny, tr, tc = shape
     geo, h0, hu0, hv0, b0 = swe.init_domain(10, nx, ny, 1, [1000.0, 100.0, 15.0, 10.0, 0.0])
     args = (geo["nx_cols"], geo["ny_rows"], geo["dx"], geo["dy"], geo["boundary"], SOLVERS[solver], h0, hu0, hv0,
             b0, 10)
-    gpu, gdts = gpu_run(swe, *args, semantics=1, mode=mode, tile_rows=tr, tile_cols=tc, variant=variant)
+    gpu, gdts = gpu_run(swe, *args, semantics=1, mode=mode, tile_rows=tr, tile_cols=tc)
     ref, rdts = oracle_run(oracle_mod, *args, semantics=1, mode=mode)
     assert_bitwise(gdts, rdts.astype(np.float32), "dt")
     compare(gpu, ref, "split %s mode %d" % (solver, mode))
