@@ -11,13 +11,14 @@
 // One launch per time step:
 //  - Column strips of h, hu, hv, b (a segment's rows plus a halo row on each
 //    side) are staged into shared memory by bulk asynchronous copies
-//    (cp.async.bulk) on a ring of kRing mbarrier slots, issued kRing columns
-//    ahead of the sweep by one thread.
-//  - Each thread owns R consecutive rows of a tile and marches along x.  The
-//    x-edge (x-1|x) uses the previous column kept in registers, the y-edges
-//    the thread's own rows and the staged row above them.  The right-going
-//    part of a thread's top y-edge reaches the thread above through shared
-//    memory; the tile's bottom y-edge of every column is solved up front.
+//    (cp.async.bulk) on a ring of kRing mbarrier slots.  The warp that
+//    releases a slot last issues the copy of the column kRing ahead.
+//  - Each thread owns two consecutive rows of a tile, computed as packed
+//    pairs (f32x2 add / mul / fma), and marches along x.  The x-edge (x-1|x)
+//    uses the previous column kept in registers, the y-edges the thread's
+//    own rows and the staged row above them.  The right-going part of a
+//    thread's top y-edge reaches the thread above by a shuffle; lane 0
+//    solves the warp's bottom y-edge itself.
 //  - The next step's maximum wave speed (computeNumericalFluxes :391-456 on
 //    Q^{n+1}) is evaluated while Q^{n+1} is produced: edges between two cells
 //    of the segment as soon as both exist, edges to a ghost from the boundary
@@ -27,6 +28,7 @@
 //    last CTA turns the maximum into the next maxTimestep (:448-456), so a
 //    step is this one kernel: no speed pass.
 #include <cfloat>
+#include <type_traits>
 
 #include "swe_fast.hpp"
 #include "swe_launch.hpp"
@@ -35,7 +37,7 @@
 namespace swegb {
 namespace fast {
 
-constexpr int kRing = 6;                          // column strips in flight per CTA
+constexpr int kRing = 4;                          // column strips in flight per CTA (4 ran faster than 5, 6, 8)
 constexpr int kHalo = 4;                          // staged rows below the tile (16-byte aligned start)
 constexpr int kSlice = kMaxTileRows + 2 * kHalo;  // floats per field of one strip
 constexpr int kSlotFloats = 4 * kSlice;           // h, hu, hv, b
@@ -333,43 +335,168 @@ __device__ __noinline__ float rimCell(float *HO, float *HUO, float *HVO, const f
 }
 
 // ---------------------------------------------------------------------------
+// packed pairs: a thread's two rows, one f32x2 instruction per operation
+// ---------------------------------------------------------------------------
+#define SWE_F2_OP2(name, op)                                                                            \
+    __device__ __forceinline__ float2 name(float2 a, float2 b) {                                        \
+        float2 d;                                                                                       \
+        asm("{\n\t.reg .b64 a, b, d;\n\tmov.b64 a, {%2, %3};\n\tmov.b64 b, {%4, %5};\n\t" op            \
+            " d, a, b;\n\tmov.b64 {%0, %1}, d;\n\t}"                                                    \
+            : "=f"(d.x), "=f"(d.y)                                                                      \
+            : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));                                                  \
+        return d;                                                                                       \
+    }
+SWE_F2_OP2(add2, "add.rn.ftz.f32x2")
+SWE_F2_OP2(sub2, "sub.rn.ftz.f32x2")
+SWE_F2_OP2(mul2, "mul.rn.ftz.f32x2")
+#undef SWE_F2_OP2
+/// a * b + c, one rounding per lane
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
+    float2 d;
+    asm("{\n\t.reg .b64 a, b, c, d;\n\tmov.b64 a, {%2, %3};\n\tmov.b64 b, {%4, %5};\n\tmov.b64 c, {%6, %7};\n\t"
+        "fma.rn.ftz.f32x2 d, a, b, c;\n\tmov.b64 {%0, %1}, d;\n\t}"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+    return d;
+}
+__device__ __forceinline__ float2 pk(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 rsqrt2(float2 a) { return make_float2(aRsqrt(a.x), aRsqrt(a.y)); }
+__device__ __forceinline__ float2 rcp2(float2 a) { return make_float2(aRcp(a.x), aRcp(a.y)); }
+__device__ __forceinline__ float2 sqrt2(float2 a) { return make_float2(aSqrt(a.x), aSqrt(a.y)); }
+
+/// FQ of two cells, one per lane of the pair
+struct FQ2 {
+    float2 h, hn, eta, u, sq, m, lo, hi;
+};
+__device__ __forceinline__ FQ2 makeFQ2(float2 h, float2 hn, float2 eta, float2 ih, float2 sq, float2 c) {
+    FQ2 q;
+    q.h = h;
+    q.hn = hn;
+    q.eta = eta;
+    q.u = mul2(hn, ih);
+    q.sq = sq;
+    q.m = mul2(hn, q.u);
+    q.lo = sub2(q.u, c);
+    q.hi = add2(q.u, c);
+    return q;
+}
+__device__ __forceinline__ FQ laneX(const FQ2 &q) { return FQ{q.h.x, q.hn.x, q.eta.x, q.u.x, q.sq.x, q.m.x, q.lo.x, q.hi.x}; }
+__device__ __forceinline__ FQ laneY(const FQ2 &q) { return FQ{q.h.y, q.hn.y, q.eta.y, q.u.y, q.sq.y, q.m.y, q.lo.y, q.hi.y}; }
+/// the pair (a, b) of two single cells
+__device__ __forceinline__ FQ2 pairFQ(const FQ &a, const FQ &b) {
+    FQ2 q;
+    q.h = make_float2(a.h, b.h);
+    q.hn = make_float2(a.hn, b.hn);
+    q.eta = make_float2(a.eta, b.eta);
+    q.u = make_float2(a.u, b.u);
+    q.sq = make_float2(a.sq, b.sq);
+    q.m = make_float2(a.m, b.m);
+    q.lo = make_float2(a.lo, b.lo);
+    q.hi = make_float2(a.hi, b.hi);
+    return q;
+}
+
+/// waves<S, false> of two edges at once, rounding as the single-edge form:
+/// the flux jump enters negated (-df2) so that both wave strengths are one
+/// fused multiply-add each, (s2 df1 - df2) / (s2 - s1) and
+/// (s1 df1 - df2) / (s1 - s2)
+template <int S>
+__device__ __forceinline__ void waves2(const FQ2 &L, const FQ2 &R, float2 &aL, float2 &aR, float2 &auL, float2 &auR,
+                                       float &sub) {
+    const float2 rs = rcp2(add2(L.sq, R.sq));
+    const float2 uRoe = mul2(fma2(L.u, L.sq, mul2(R.u, R.sq)), rs);
+    const float2 ghs = mul2(pk(kHalfG), add2(L.h, R.h));
+    const float2 cRoe = sqrt2(ghs);
+    float2 s1 = sub2(uRoe, cRoe), s2 = add2(uRoe, cRoe);
+    if (S == SOLVER_HLLE) {
+        s1 = make_float2(fminf(L.lo.x, s1.x), fminf(L.lo.y, s1.y));
+        s2 = make_float2(fmaxf(R.hi.x, s2.x), fmaxf(R.hi.y, s2.y));
+    }
+    const float2 df1 = sub2(R.hn, L.hn);
+    const float2 ndf2 = fma2(ghs, sub2(L.eta, R.eta), sub2(L.m, R.m));  // -(flux jump)
+    const float2 rd = rcp2(sub2(s2, s1));
+    const float2 nrd = mul2(rd, pk(-1.f));
+    aL = mul2(fma2(s2, df1, ndf2), rd);
+    aR = mul2(fma2(s1, df1, ndf2), nrd);
+    auL = mul2(aL, s1);
+    auR = mul2(aR, s2);
+    sub = fminf(sub, fminf(fminf(-s1.x, -s1.y), fminf(s2.x, s2.y)));
+}
+
+// ---------------------------------------------------------------------------
 // the step kernel
 // ---------------------------------------------------------------------------
+/// Loads of a thread's R = 2 NP consecutive rows of one strip field as NP pairs.
+template <int NP> __device__ __forceinline__ void loadRows(const float *p, float2 (&v)[NP]) {
+    if constexpr (NP == 2) {
+        const float4 a = *reinterpret_cast<const float4 *>(p);
+        v[0] = make_float2(a.x, a.y);
+        v[NP - 1] = make_float2(a.z, a.w);
+    } else {
+#pragma unroll
+        for (int q = 0; q < NP; q++) v[q] = *reinterpret_cast<const float2 *>(p + 2 * q);
+    }
+}
+/// Stores of NP pairs to R consecutive rows of a field.
+template <int NP> __device__ __forceinline__ void storeRows(float *p, const float2 (&v)[NP]) {
+    if constexpr (NP == 2) {
+        *reinterpret_cast<float4 *>(p) = make_float4(v[0].x, v[0].y, v[NP - 1].x, v[NP - 1].y);
+    } else {
+#pragma unroll
+        for (int q = 0; q < NP; q++) *reinterpret_cast<float2 *>(p + 2 * q) = v[q];
+    }
+}
+__device__ __forceinline__ float lanePick(float2 v, int i) { return i ? v.y : v.x; }
+
 /// HLLE: the next state's maximum wave speed is the largest cell speed
 /// c + max(|u|, |v|) over its wet cells -- exactly, in exact arithmetic: every
 /// edge speed is at most the larger cell speed of its two cells (|uRoe| is a
 /// sqrt(h)-weighted mean of |u|, cRoe at most the same mean of c, and the
 /// Einfeldt bounds are the cells' own u -/+ c), and every wet cell's u + c
 /// and c - u are the Einfeldt bounds of its left and right edges (v likewise
-/// in y; a dry neighbour's mirror image gives the same).  Only edges to
-/// ghosts that keep their own values need their speed evaluated.  The f-wave
-/// solver has no such identity: its edges are evaluated one by one, those
-/// between two segments as pieces.
-template <int S, int R, int MINB>
-__global__ void __launch_bounds__(kMaxTileRows / R, MINB) fastStepKernel(const FastDev f) {
+/// in y; a dry neighbour's mirror image gives the same).  A dry cell
+/// (h < dryTol, momenta cleared by the clamp) has c + 0 < sqrt(g dryTol), below
+/// every wet cell's speed, so a thread keeps the largest cell speed of all
+/// its cells and drops it when none of them was wet.  Only edges to ghosts
+/// that keep their own values need their speed evaluated.  The f-wave solver
+/// has no such identity: its edges are evaluated one by one, those between
+/// two segments as pieces.
+///
+/// Each thread owns R = 2 NP consecutive rows, computed as NP packed pairs.
+template <int S, int NP, int MINB>
+__global__ void __launch_bounds__(kMaxTileRows / (2 * NP), MINB) fastStepKernel(const FastDev f) {
+    constexpr int R = 2 * NP;
     constexpr int NT = kMaxTileRows / R;
+    constexpr int NW = (NT + 31) / 32;
     constexpr unsigned FULL = 0xffffffffu;
     constexpr bool EDGES = S == SOLVER_FWAVE;  // next-state speeds edge by edge
+    using T_ = std::true_type;
+    using F_ = std::false_type;
     extern __shared__ __align__(128) float ring[];  // kRing strips of kSlotFloats
     __shared__ __align__(8) unsigned long long mbar[kRing];
-    __shared__ int slotDone[kRing];  // warps done with the strip in a slot
-    __shared__ float sRed[NT / 32];
+    __shared__ unsigned slotDone[kRing];  // releases of a slot so far (nw per column)
+    __shared__ float sRed[NW];
+    __shared__ long long sRimGhost[NT][R];  // rim rows: the ghost row's offset from the block's base
+    __shared__ int sRimPitch[NT][R];        // and its pitch
     __shared__ int sLast, sNWon, sAbort;
     __shared__ int sWon[kMaxArrivals];
 
-    const int t = threadIdx.x, lane = t & 31, nth = blockDim.x, nw = nth >> 5, TY = nth * R;
+    const int t = threadIdx.x, lane = t & 31, nth = blockDim.x, nw = nth >> 5, TY = R * nth;
     // strips start as a state at rest (rows a partial tile never loads stay finite)
     for (int i = t; i < kRing * kSlotFloats; i += nth) ring[i] = ((i % kSlotFloats) < kSlice) ? 1.f : 0.f;
     if (t == 0) {
         for (int s = 0; s < kRing; s++) {
             mbarInit(smemAddr(&mbar[s]), 1u);
-            slotDone[s] = 0;
+            slotDone[s] = 0u;
         }
         sAbort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
-    unsigned phases = 0u;  // bit s: parity of slot s's next phase
+    // slot of the next column and the rotations so far (the slot's phase
+    // parity); the rotation continues across segments
+    int slot = 0;
+    unsigned rnd = 0u;
     pdlWaitAndRelease();
 
     const unsigned ringAddr = smemAddr(ring);
@@ -387,11 +514,11 @@ __global__ void __launch_bounds__(kMaxTileRows / R, MINB) fastStepKernel(const F
         const int y0 = wu.y0, yTop = min(y0 + TY - 1, ny);
         const int rowStart = y0 - kHalo;
         const unsigned bytes = unsigned(((yTop + 2 - rowStart) + 3) & ~3) * 4u;
-        float dtdx, dtdy;
+        float2 dtdx, dtdy;
         {
             const float dt = __ldg(&G->dt);
-            dtdx = __fdiv_rn(dt, __ldg(&B.dx));
-            dtdy = __fdiv_rn(dt, __ldg(&B.dy));
+            dtdx = pk(__fdiv_rn(dt, __ldg(&B.dx)));
+            dtdy = pk(__fdiv_rn(dt, __ldg(&B.dy)));
         }
         const float *__restrict__ Hin = pick(f.d.h, cur);
         const float *__restrict__ HUin = pick(f.d.hu, cur);
@@ -399,12 +526,13 @@ __global__ void __launch_bounds__(kMaxTileRows / R, MINB) fastStepKernel(const F
         float *__restrict__ HO = pick(f.d.h, cur ^ 1) + base;
         float *__restrict__ HUO = pick(f.d.hu, cur ^ 1) + base;
         float *__restrict__ HVO = pick(f.d.hv, cur ^ 1) + base;
-        // the strip of column x0-1+k (rows rowStart ..) into slot k % kRing
-        auto refill = [&](int k, int slot) {
-            const unsigned mb = smemAddr(&mbar[slot]);
+        const int slot0 = slot;
+        // the strip of column x0-1+k (rows rowStart ..) into slot s
+        auto refill = [&](int k, int s) {
+            const unsigned mb = smemAddr(&mbar[s]);
             mbarExpectTx(mb, 4u * bytes);
             const size_t col = size_t(base) + size_t(x0 - 1 + k) * P + size_t(rowStart);
-            const unsigned dst = ringAddr + unsigned(slot * kSlotFloats) * 4u;
+            const unsigned dst = ringAddr + unsigned(s * kSlotFloats) * 4u;
             bulkLoad(dst, Hin + col, bytes, mb);
             bulkLoad(dst + unsigned(kSlice) * 4u, HUin + col, bytes, mb);
             bulkLoad(dst + unsigned(2 * kSlice) * 4u, HVin + col, bytes, mb);
@@ -414,7 +542,7 @@ __global__ void __launch_bounds__(kMaxTileRows / R, MINB) fastStepKernel(const F
         __syncthreads();  // the previous segment is done with every slot and shared value
         if (t == 0) {
             sNWon = 0;
-            for (int k = 0; k < min(kRing, ncol); k++) refill(k, k);
+            for (int k = 0; k < min(kRing, ncol); k++) refill(k, slot0 + k < kRing ? slot0 + k : slot0 + k - kRing);
         }
 
         const int yA = y0 + R * t;                       // this thread's first row
@@ -422,233 +550,262 @@ __global__ void __launch_bounds__(kMaxTileRows / R, MINB) fastStepKernel(const F
         const bool fullTile = yTop - y0 + 1 == TY;       // every thread has R rows (CTA-uniform)
         const bool upIn = yA + R <= yTop;                // the next thread's first row is in the tile
         // rows on the block's rim (y == 1, y == ny): ghost below / above.
-        // rimMode per row: 0 none, 1 copy, 2 copy with -hv, 3 kept ghost (its
-        // edge speed is evaluated), 4 every ghost edge evaluated (f-wave)
-        int rimMode[R];
-        long long rimGhost[R];
-        int rimPitch[R];
+        // rimMode (3 bits per row): 0 none, 1 copy, 2 copy with -hv, 3 kept
+        // ghost (its edge speed is evaluated), 4 every ghost edge evaluated
+        // (f-wave); the ghost row's offset and pitch wait in shared memory
+        int rimModes = 0;
         bool rimAny = false;
 #pragma unroll
         for (int r = 0; r < R; r++) {
             const int y = yA + r;
-            rimMode[r] = 0;
-            rimGhost[r] = 0;
-            rimPitch[r] = 0;
             if (r < nAct && (y == 1 || y == ny)) {
                 rimAny = true;
                 const int side = (y == 1) ? 2 : 3;
                 const int type = __ldg(&B.bnd[side]);
-                rimGhost[r] = (side == 2) ? 0 : ny + 1;
-                rimPitch[r] = int(P);
+                long long ghost = (side == 2) ? 0 : ny + 1;
+                int pitch = int(P), mode;
                 if (ny == 1 || EDGES) {
-                    rimMode[r] = 4;
+                    mode = 4;
                 } else if (type == OUTFLOW || type == WALL) {
-                    rimMode[r] = type == WALL ? 2 : 1;
+                    mode = type == WALL ? 2 : 1;
                 } else if (type == CONNECT_WITHIN_RANK) {
                     const BlockDesc &N = f.d.blocks[__ldg(&B.nbr[side])];
-                    rimMode[r] = 1;
-                    rimGhost[r] = __ldg(&N.base) - base + ((side == 2) ? __ldg(&N.ny) + 1 : 0);
-                    rimPitch[r] = __ldg(&N.pitch);
+                    mode = 1;
+                    ghost = __ldg(&N.base) - base + ((side == 2) ? __ldg(&N.ny) + 1 : 0);
+                    pitch = __ldg(&N.pitch);
                 } else {
-                    rimMode[r] = 3;
+                    mode = 3;
                 }
+                rimModes |= mode << (3 * r);
+                sRimGhost[t][r] = ghost;
+                sRimPitch[t][r] = pitch;
             }
         }
         const bool rimWarp = __any_sync(FULL, rimAny);
 
-        FQ prevX[R];
-        float pendH[R], pendHU[R], oldHV[R], syH[R], syHV[R];
+        FQ2 px[NP];                                      // the previous column's cells (x direction)
+        float2 pendH[NP], pendHU[NP];                    // right-going parts of their left x-edges
+        float2 syH[NP], syHV[NP], oldHV[NP];             // their y sums and hv
+        float2 hsum = pk(0.f);                           // new depths (not finite: a non-finite cell)
+        float smax = 0.f, wmax = 0.f, hmax = 0.f;        // edge speeds; HLLE cell speeds and depths
         SV nprev[R];
-        float smax = 0.f;
-        bool bad = false;
 #pragma unroll
-        for (int r = 0; r < R; r++) {
-            pendH[r] = pendHU[r] = oldHV[r] = syH[r] = syHV[r] = 0.f;
-            nprev[r] = SV{1.f, 0.f, 1.f, 0.f};
-        }
+        for (int q = 0; q < NP; q++) pendH[q] = pendHU[q] = syH[q] = syHV[q] = oldHV[q] = pk(0.f);
+#pragma unroll
+        for (int r = 0; r < R; r++) nprev[r] = SV{1.f, 0.f, 1.f, 0.f};
         const int i0 = kHalo + R * t;  // strip index of this thread's first row
-        int slot = 0;
-        for (int k = 0; k < ncol; ++k) {
-            // wait for the strip of column x = x0-1+k (bounded; a stalled copy
-            // aborts the CTA, see below)
+        unsigned oldPrev = 0u;         // lane 0: the previous column's release count
+
+        // one column x = x0-1+k: XCOL its x-edges (x-1 | x), YCOL its y-edges,
+        // UPD the update of column x-1, RIMX column x-1 may be on the block's
+        // left or right rim.  False: a copy did not arrive in time.
+        auto column = [&](int k, auto xcolT, auto ycolT, auto updT, auto rimxT) -> bool {
+            constexpr bool XCOL = decltype(xcolT)::value, YCOL = decltype(ycolT)::value;
+            constexpr bool UPD = decltype(updT)::value, RIMX = decltype(rimxT)::value;
+            // wait for the strip (bounded; a stalled copy aborts the CTA)
             {
-                const unsigned a = smemAddr(&mbar[slot]), par = (phases >> slot) & 1u;
-                bool ok = mbarTryWait(a, par);
-                for (unsigned n = 0; !ok && n < kSpinLimit; ++n) {
-                    if (*(volatile int *)&sAbort) break;
-                    ok = mbarTryWait(a, par);
+                const unsigned a = smemAddr(&mbar[slot]);
+                const unsigned par = rnd & 1u;
+                if (!__all_sync(FULL, mbarTryWait(a, par))) {
+                    bool ok = false;
+                    for (unsigned n = 0; !ok && n < kSpinLimit; ++n) {
+                        if (*(volatile int *)&sAbort) break;
+                        ok = __all_sync(FULL, mbarTryWait(a, par));
+                    }
+                    if (!ok) {
+                        if (lane == 0) *(volatile int *)&sAbort = 1;
+                        return false;
+                    }
                 }
-                if (__any_sync(FULL, !ok)) {
-                    if (lane == 0) *(volatile int *)&sAbort = 1;
-                    break;
-                }
-                phases ^= 1u << slot;
             }
             const float *sl = ring + slot * kSlotFloats;
-            // A. this thread's cells of column x
-            float ch[R], chu[R], chv[R], cb[R];
-            if (R == 4) {
-                const float4 a = *reinterpret_cast<const float4 *>(sl + i0);
-                const float4 bq = *reinterpret_cast<const float4 *>(sl + kSlice + i0);
-                const float4 c = *reinterpret_cast<const float4 *>(sl + 2 * kSlice + i0);
-                const float4 e = *reinterpret_cast<const float4 *>(sl + 3 * kSlice + i0);
-                const float va[4] = {a.x, a.y, a.z, a.w}, vb[4] = {bq.x, bq.y, bq.z, bq.w};
-                const float vc[4] = {c.x, c.y, c.z, c.w}, ve[4] = {e.x, e.y, e.z, e.w};
-#pragma unroll
-                for (int r = 0; r < R; r++) {
-                    ch[r] = va[r % 4]; chu[r] = vb[r % 4]; chv[r] = vc[r % 4]; cb[r] = ve[r % 4];
-                }
-            } else if (R == 2) {
-                const float2 a = *reinterpret_cast<const float2 *>(sl + i0);
-                const float2 bq = *reinterpret_cast<const float2 *>(sl + kSlice + i0);
-                const float2 c = *reinterpret_cast<const float2 *>(sl + 2 * kSlice + i0);
-                const float2 e = *reinterpret_cast<const float2 *>(sl + 3 * kSlice + i0);
-                ch[0] = a.x; ch[R - 1] = a.y;
-                chu[0] = bq.x; chu[R - 1] = bq.y;
-                chv[0] = c.x; chv[R - 1] = c.y;
-                cb[0] = e.x; cb[R - 1] = e.y;
-            } else {
-#pragma unroll
-                for (int r = 0; r < R; r++) {
-                    ch[r] = sl[i0 + r];
-                    chu[r] = sl[kSlice + i0 + r];
-                    chv[r] = sl[2 * kSlice + i0 + r];
-                    cb[r] = sl[3 * kSlice + i0 + r];
+            float2 ch[NP], chu[NP], chv[NP], cb[NP];
+            loadRows<NP>(sl + i0, ch);
+            loadRows<NP>(sl + kSlice + i0, chu);
+            loadRows<NP>(sl + 2 * kSlice + i0, chv);
+            loadRows<NP>(sl + 3 * kSlice + i0, cb);
+            float uh = 0.f, uhv = 0.f, ub = 0.f, lh = 0.f, lhv = 0.f, lb = 0.f;
+            if (YCOL) {
+                uh = sl[i0 + R];
+                uhv = sl[2 * kSlice + i0 + R];
+                ub = sl[3 * kSlice + i0 + R];
+                if (lane == 0) {  // the cell below the warp's first row
+                    lh = sl[i0 - 1];
+                    lhv = sl[2 * kSlice + i0 - 1];
+                    lb = sl[3 * kSlice + i0 - 1];
                 }
             }
-            FQ cx[R], cy[R];
-            float minh = 3.0e38f;  // smallest depth the column's edges touch
+            // A. this thread's cells of column x, the cell above its rows and
+            // (lane 0) the one below
+            FQ2 cx[NP], cy[NP];
 #pragma unroll
-            for (int r = 0; r < R; r++) {
-                const float rr = aRsqrt(ch[r]);
-                const float sq = ch[r] * rr, ih = rr * rr, c = kSqrtG * sq, eta = ch[r] + cb[r];
-                cx[r] = makeFQ(ch[r], chu[r], eta, ih, sq, c);
-                cy[r] = makeFQ(ch[r], chv[r], eta, ih, sq, c);
-                minh = fminf(minh, ch[r]);
+            for (int q = 0; q < NP; q++) {
+                const float2 rr = rsqrt2(ch[q]);
+                const float2 sq = mul2(ch[q], rr), ih = mul2(rr, rr), c = mul2(pk(kSqrtG), sq);
+                const float2 eta = add2(ch[q], cb[q]);
+                cx[q] = makeFQ2(ch[q], chu[q], eta, ih, sq, c);
+                cy[q] = makeFQ2(ch[q], chv[q], eta, ih, sq, c);
             }
-            const bool xcol = k >= 1, ycol = k >= 1 && k <= XC;
-            // B. x-edges (x-1 | x); y-edges of column x: between this thread's
-            // rows and the top one with the staged row above; lane 0 also the
-            // one below its first row (its right-going part comes from no
-            // other lane).  All taken as wet and subsonic first.
-            float aLx[R], aRx[R], auLx[R], auRx[R], bLh[R], bLhv[R], bRh[R], bRhv[R], tRh = 0.f, tRhv = 0.f;
+            FQ up{}, low{};
+            if (YCOL) {
+                up = rawFQ(uh, uhv, ub);
+                if (lane == 0) low = rawFQ(lh, lhv, lb);
+            }
+            // the strip's values are in use, so its reads are complete:
+            // release it.  The slot's last releaser refills it; lane 0 reads
+            // its count one column later, so no warp waits on the atomic.
+            __syncwarp();
+            if (lane == 0) {
+                if (k >= 1 && k - 1 + kRing < ncol) {
+                    const int sp = slot == 0 ? kRing - 1 : slot - 1;
+                    const unsigned rp = slot == 0 ? rnd - 1u : rnd;
+                    if (oldPrev + 1u == unsigned(nw) * (rp + 1u)) refill(k - 1 + kRing, sp);
+                }
+                unsigned old;
+                asm volatile("atom.shared::cta.add.u32 %0, [%1], 1;"
+                             : "=r"(old)
+                             : "r"(smemAddr(&slotDone[slot])), "f"(cx[0].m.x), "f"(cx[0].m.y), "f"(cy[0].m.x),
+                               "f"(cy[0].m.y), "f"(cx[0].eta.x), "f"(cx[0].eta.y), "f"(up.m), "f"(up.eta), "f"(low.m),
+                               "f"(low.eta)
+                             : "memory");
+                oldPrev = old;
+            }
+            if (++slot == kRing) {
+                slot = 0;
+                ++rnd;
+            }
+            // B. x-edges (x-1 | x) and the y-edges between this thread's rows
+            // and from its last row to the staged row above (lane 0: also the
+            // one below its first row), all taken as wet and subsonic first
+            float2 aLx[NP], aRx[NP], auLx[NP], auRx[NP], aLy[NP], aRy[NP], auLy[NP], auRy[NP];
+            float sub = 3.0e38f, minh = 3.0e38f;
+#pragma unroll
+            for (int q = 0; q < NP; q++) minh = fminf(minh, fminf(ch[q].x, ch[q].y));
+            if (XCOL) {
+#pragma unroll
+                for (int q = 0; q < NP; q++) {
+                    waves2<S>(px[q], cx[q], aLx[q], aRx[q], auLx[q], auRx[q], sub);
+                    minh = fminf(minh, fminf(px[q].h.x, px[q].h.y));
+                }
+            }
             float lowRh = 0.f, lowRhv = 0.f;
-            float sub = 3.0e38f;
-            FQ up, low;
-            if (xcol) {
+            if (YCOL) {
 #pragma unroll
-                for (int r = 0; r < R; r++) {
-                    waves<S, false>(prevX[r], cx[r], aLx[r], aRx[r], auLx[r], auRx[r], sub);
-                    minh = fminf(minh, prevX[r].h);
-                }
-            }
-            if (ycol) {
-                const int iu = i0 + R;
-                up = rawFQ(sl[iu], sl[2 * kSlice + iu], sl[3 * kSlice + iu]);
-#pragma unroll
-                for (int r = 0; r + 1 < R; r++)
-                    waves<S, false>(cy[r], cy[(r + 1) % R], bLh[r], bRh[(r + 1) % R], bLhv[r], bRhv[(r + 1) % R], sub);
-                waves<S, false>(cy[R - 1], up, bLh[R - 1], tRh, bLhv[R - 1], tRhv, sub);
+                for (int q = 0; q < NP; q++)
+                    waves2<S>(cy[q], pairFQ(laneY(cy[q]), q + 1 < NP ? laneX(cy[(q + 1) % NP]) : up), aLy[q], aRy[q],
+                              auLy[q], auRy[q], sub);
                 minh = fminf(minh, up.h);
                 if (lane == 0) {
-                    low = rawFQ(sl[i0 - 1], sl[2 * kSlice + i0 - 1], sl[3 * kSlice + i0 - 1]);
                     float dl, dlv;
-                    waves<S, false>(low, cy[0], dl, lowRh, dlv, lowRhv, sub);
+                    waves<S, false>(low, laneX(cy[0]), dl, lowRh, dlv, lowRhv, sub);
                     minh = fminf(minh, low.h);
                 }
             }
-            // the strip is read: the warp that finishes it last refills the slot
-            __syncwarp();
-            if (lane == 0) {
-                if (atomicAdd(&slotDone[slot], 1) == nw - 1) {
-                    slotDone[slot] = 0;
-                    if (k + kRing < ncol) refill(k + kRing, slot);
-                }
-            }
-            slot = (slot + 1 == kRing) ? 0 : slot + 1;
             // C. a lane with a dry cell or an edge that is not subsonic solves
             // its edges again in full (rare: shorelines, fronts)
-            const bool redo = xcol && (minh < kDryTol || !(sub > kZeroTol));
-            if (__any_sync(FULL, redo)) {
-                if (redo) {
+            if (XCOL || YCOL) {
+                const bool redo = minh < kDryTol || !(sub > kZeroTol);
+                if (__any_sync(FULL, redo)) {
+                    if (redo) {
+                        if (XCOL) {
 #pragma unroll
-                    for (int r = 0; r < R; r++) {
-                        const float4 e = edgeGeneral<S>(prevX[r], cx[r]);
-                        aLx[r] = e.x; aRx[r] = e.y; auLx[r] = e.z; auRx[r] = e.w;
-                    }
-                    if (ycol) {
-#pragma unroll
-                        for (int r = 0; r + 1 < R; r++) {
-                            const float4 e = edgeGeneral<S>(cy[r], cy[(r + 1) % R]);
-                            bLh[r] = e.x; bRh[(r + 1) % R] = e.y; bLhv[r] = e.z; bRhv[(r + 1) % R] = e.w;
+                            for (int q = 0; q < NP; q++) {
+                                const float4 e0 = edgeGeneral<S>(laneX(px[q]), laneX(cx[q]));
+                                const float4 e1 = edgeGeneral<S>(laneY(px[q]), laneY(cx[q]));
+                                aLx[q] = make_float2(e0.x, e1.x);
+                                aRx[q] = make_float2(e0.y, e1.y);
+                                auLx[q] = make_float2(e0.z, e1.z);
+                                auRx[q] = make_float2(e0.w, e1.w);
+                            }
                         }
-                        const float4 e = edgeGeneral<S>(cy[R - 1], up);
-                        bLh[R - 1] = e.x; tRh = e.y; bLhv[R - 1] = e.z; tRhv = e.w;
-                        if (lane == 0) {
-                            const float4 e0 = edgeGeneral<S>(low, cy[0]);
-                            lowRh = e0.y;
-                            lowRhv = e0.w;
+                        if (YCOL) {
+#pragma unroll
+                            for (int q = 0; q < NP; q++) {
+                                const float4 e0 = edgeGeneral<S>(laneX(cy[q]), laneY(cy[q]));
+                                const float4 e1 =
+                                    edgeGeneral<S>(laneY(cy[q]), q + 1 < NP ? laneX(cy[(q + 1) % NP]) : up);
+                                aLy[q] = make_float2(e0.x, e1.x);
+                                aRy[q] = make_float2(e0.y, e1.y);
+                                auLy[q] = make_float2(e0.z, e1.z);
+                                auRy[q] = make_float2(e0.w, e1.w);
+                            }
+                            if (lane == 0) {
+                                const float4 e2 = edgeGeneral<S>(low, laneX(cy[0]));
+                                lowRh = e2.y;
+                                lowRhv = e2.w;
+                            }
                         }
                     }
                 }
             }
             // D. cells (x-1, y): Q^{n+1} with the dry clamp, and their part
             // of the next maxTimestep
-            if (k >= 2) {
+            if (UPD) {
                 const int xc = x0 - 2 + k;
-                float hn[R], hun[R], hvn[R];
+                float2 hn[NP], hun[NP], hvn[NP];
 #pragma unroll
-                for (int r = 0; r < R; r++) {
-                    const float sxH = pendH[r] + aLx[r], sxHU = pendHU[r] + auLx[r];
-                    float h_ = prevX[r].h - (dtdx * sxH + dtdy * syH[r]);
-                    float hu_ = prevX[r].hn - dtdx * sxHU;
-                    float hv_ = oldHV[r] - dtdy * syHV[r];
-                    hu_ = (h_ < 0.1f) ? 0.f : hu_;
-                    hv_ = (h_ < 0.1f) ? 0.f : hv_;
-                    h_ = (h_ < 0.f) ? 0.f : h_;
-                    hn[r] = h_;
-                    hun[r] = hu_;
-                    hvn[r] = hv_;
-                    bad |= (r < nAct) && !(fabsf(h_) <= FLT_MAX);
+                for (int q = 0; q < NP; q++) {
+                    hn[q] = sub2(px[q].h, fma2(dtdx, add2(pendH[q], aLx[q]), mul2(dtdy, syH[q])));
+                    hun[q] = sub2(px[q].hn, mul2(dtdx, add2(pendHU[q], auLx[q])));
+                    hvn[q] = sub2(oldHV[q], mul2(dtdy, syHV[q]));
+                    if (fullTile) {
+                        hsum = add2(hsum, hn[q]);
+                    } else {
+                        hsum.x += 2 * q < nAct ? hn[q].x : 0.f;
+                        hsum.y += 2 * q + 1 < nAct ? hn[q].y : 0.f;
+                    }
+                    hun[q].x = (hn[q].x < 0.1f) ? 0.f : hun[q].x;
+                    hvn[q].x = (hn[q].x < 0.1f) ? 0.f : hvn[q].x;
+                    hun[q].y = (hn[q].y < 0.1f) ? 0.f : hun[q].y;
+                    hvn[q].y = (hn[q].y < 0.1f) ? 0.f : hvn[q].y;
+                    hn[q].x = fmaxf(hn[q].x, 0.f);
+                    hn[q].y = fmaxf(hn[q].y, 0.f);
                 }
                 const unsigned o = unsigned(xc) * P + unsigned(yA);
-                if (R == 4 && fullTile) {
-                    *reinterpret_cast<float4 *>(HO + o) = make_float4(hn[0], hn[1 % R], hn[2 % R], hn[3 % R]);
-                    *reinterpret_cast<float4 *>(HUO + o) = make_float4(hun[0], hun[1 % R], hun[2 % R], hun[3 % R]);
-                    *reinterpret_cast<float4 *>(HVO + o) = make_float4(hvn[0], hvn[1 % R], hvn[2 % R], hvn[3 % R]);
-                } else if (R == 2 && fullTile) {
-                    *reinterpret_cast<float2 *>(HO + o) = make_float2(hn[0], hn[R - 1]);
-                    *reinterpret_cast<float2 *>(HUO + o) = make_float2(hun[0], hun[R - 1]);
-                    *reinterpret_cast<float2 *>(HVO + o) = make_float2(hvn[0], hvn[R - 1]);
+                if (fullTile) {
+                    storeRows<NP>(HO + o, hn);
+                    storeRows<NP>(HUO + o, hun);
+                    storeRows<NP>(HVO + o, hvn);
                 } else {
 #pragma unroll
                     for (int r = 0; r < R; r++)
                         if (r < nAct) {
-                            HO[o + r] = hn[r];
-                            HUO[o + r] = hun[r];
-                            HVO[o + r] = hvn[r];
+                            HO[o + r] = lanePick(hn[r / 2], r & 1);
+                            HUO[o + r] = lanePick(hun[r / 2], r & 1);
+                            HVO[o + r] = lanePick(hvn[r / 2], r & 1);
                         }
                 }
-                if (!EDGES) {
-                    // HLLE: the wet new cells' speeds c + max(|u|, |v|)
+                float2 rn[NP];
 #pragma unroll
-                    for (int r = 0; r < R; r++) {
-                        const float rn = aRsqrt(hn[r]);
-                        const float w = fmaf(fmaxf(fabsf(hun[r]), fabsf(hvn[r])), rn * rn, kSqrtG * (hn[r] * rn));
-                        smax = fmaxf(smax, (r < nAct && hn[r] >= kDryTol) ? w : 0.f);
+                for (int q = 0; q < NP; q++) rn[q] = rsqrt2(hn[q]);
+                if (!EDGES) {
+                    // HLLE: cell speeds c + max(|u|, |v|) (a dry cell: NaN for
+                    // h = 0, below every wet cell's speed otherwise)
+#pragma unroll
+                    for (int q = 0; q < NP; q++) {
+                        const float2 vmax = make_float2(fmaxf(fabsf(hun[q].x), fabsf(hvn[q].x)),
+                                                        fmaxf(fabsf(hun[q].y), fabsf(hvn[q].y)));
+                        const float2 w = fma2(vmax, mul2(rn[q], rn[q]), mul2(pk(kSqrtG), mul2(hn[q], rn[q])));
+                        if (fullTile) {
+                            wmax = fmaxf(wmax, fmaxf(w.x, w.y));
+                            hmax = fmaxf(hmax, fmaxf(hn[q].x, hn[q].y));
+                        } else {
+                            wmax = fmaxf(wmax, fmaxf(2 * q < nAct ? w.x : 0.f, 2 * q + 1 < nAct ? w.y : 0.f));
+                            hmax = fmaxf(hmax, fmaxf(2 * q < nAct ? hn[q].x : 0.f, 2 * q + 1 < nAct ? hn[q].y : 0.f));
+                        }
                     }
                 } else {
-                    // f-wave: x-edge (x-2 | x-1), the y-edges between this
+                    // f-wave: x-edges (x-2 | x-1), the y-edges between this
                     // thread's rows and the one to the next lane's first row
                     // (the last lane's goes to the pass after the sweep)
                     SV nxv[R], nyv[R];
                     float nminh = 3.0e38f;
 #pragma unroll
                     for (int r = 0; r < R; r++) {
-                        const float rn = aRsqrt(hn[r]);
-                        nxv[r] = makeSV(hn[r], hun[r], rn);
-                        nyv[r] = makeSV(hn[r], hvn[r], rn);
-                        nminh = fminf(nminh, fminf(hn[r], nprev[r].h));
+                        const float hr = lanePick(hn[r / 2], r & 1), rr2 = lanePick(rn[r / 2], r & 1);
+                        nxv[r] = makeSV(hr, lanePick(hun[r / 2], r & 1), rr2);
+                        nyv[r] = makeSV(hr, lanePick(hvn[r / 2], r & 1), rr2);
+                        nminh = fminf(nminh, fminf(hr, nprev[r].h));
                     }
                     SV nu;
                     nu.h = __shfl_down_sync(FULL, nyv[0].h, 1);
@@ -661,7 +818,7 @@ __global__ void __launch_bounds__(kMaxTileRows / R, MINB) fastStepKernel(const F
 #pragma unroll
                     for (int r = 0; r < R; r++) sp[r] = wetSpeed<S>(nprev[r], nxv[r]);
 #pragma unroll
-                    for (int r = 0; r + 1 < R; r++) sp[R + r] = wetSpeed<S>(nyv[r], nyv[(r + 1) % R]);
+                    for (int r = 0; r + 1 < R; r++) sp[R + r] = wetSpeed<S>(nyv[r], nyv[r + 1]);
                     sp[2 * R] = wetSpeed<S>(nyv[R - 1], nu);
                     const bool nredo = nminh < kDryTol;
                     if (__any_sync(FULL, nredo)) {
@@ -669,7 +826,7 @@ __global__ void __launch_bounds__(kMaxTileRows / R, MINB) fastStepKernel(const F
 #pragma unroll
                             for (int r = 0; r < R; r++) sp[r] = speedGeneral<S>(nprev[r], nxv[r]);
 #pragma unroll
-                            for (int r = 0; r + 1 < R; r++) sp[R + r] = speedGeneral<S>(nyv[r], nyv[(r + 1) % R]);
+                            for (int r = 0; r + 1 < R; r++) sp[R + r] = speedGeneral<S>(nyv[r], nyv[r + 1]);
                             sp[2 * R] = speedGeneral<S>(nyv[R - 1], nu);
                         }
                     }
@@ -682,60 +839,71 @@ __global__ void __launch_bounds__(kMaxTileRows / R, MINB) fastStepKernel(const F
                     for (int r = 0; r < R; r++) nprev[r] = nxv[r];
                 }
                 // the block's rim: ghost pushes, edges to the block's own ghosts
-                if (xc == 1 || xc == nx) {
+                if (RIMX && (xc == 1 || xc == nx)) {
 #pragma unroll
                     for (int r = 0; r < R; r++)
                         if (r < nAct)
                             smax = fmaxf(smax, rimCell<S>(pick(f.d.h, cur ^ 1), pick(f.d.hu, cur ^ 1), pick(f.d.hv, cur ^ 1),
-                                                          Hin, HUin, HVin, f.d.blocks, wu.block, xc, yA + r, hn[r],
-                                                          hun[r], hvn[r]));
+                                                          Hin, HUin, HVin, f.d.blocks, wu.block, xc, yA + r,
+                                                          lanePick(hn[r / 2], r & 1), lanePick(hun[r / 2], r & 1),
+                                                          lanePick(hvn[r / 2], r & 1)));
                 } else if (rimWarp) {
 #pragma unroll
                     for (int r = 0; r < R; r++) {
-                        if (rimMode[r] == 0) continue;
-                        if (rimMode[r] >= 3) {
+                        const int mode = (rimModes >> (3 * r)) & 7;
+                        if (mode == 0) continue;
+                        const float hr = lanePick(hn[r / 2], r & 1), ur = lanePick(hun[r / 2], r & 1),
+                                    vr = lanePick(hvn[r / 2], r & 1);
+                        if (mode >= 3) {
                             smax = fmaxf(smax, rimCell<S>(pick(f.d.h, cur ^ 1), pick(f.d.hu, cur ^ 1), pick(f.d.hv, cur ^ 1),
-                                                          Hin, HUin, HVin, f.d.blocks, wu.block, xc, yA + r, hn[r],
-                                                          hun[r], hvn[r]));
+                                                          Hin, HUin, HVin, f.d.blocks, wu.block, xc, yA + r, hr, ur, vr));
                         } else {
-                            const long long g = rimGhost[r] + (long long)xc * rimPitch[r];
-                            HO[g] = hn[r];
-                            HUO[g] = hun[r];
-                            HVO[g] = rimMode[r] == 2 ? -hvn[r] : hvn[r];
+                            const long long g = sRimGhost[t][r] + (long long)xc * sRimPitch[t][r];
+                            HO[g] = hr;
+                            HUO[g] = ur;
+                            HVO[g] = mode == 2 ? -vr : vr;
                         }
                     }
                 }
             }
-            if (ycol) {
-                // y-sums of column x: right-going part of the edge below the
-                // first row from the lane below (lane 0: its own), left-going
-                // parts from this lane's edges
-                const float pH = __shfl_up_sync(FULL, tRh, 1), pHV = __shfl_up_sync(FULL, tRhv, 1);
-                bRh[0] = (lane == 0) ? lowRh : pH;
-                bRhv[0] = (lane == 0) ? lowRhv : pHV;
+            if (YCOL) {
+                // y-sums of column x: the first row's bottom edge from the
+                // lane below (lane 0: its own), the rest from this lane's edges
+                const float pH = __shfl_up_sync(FULL, aRy[NP - 1].y, 1), pHV = __shfl_up_sync(FULL, auRy[NP - 1].y, 1);
 #pragma unroll
-                for (int r = 0; r < R; r++) {
-                    syH[r] = bRh[r] + bLh[r];
-                    syHV[r] = bRhv[r] + bLhv[r];
-                    oldHV[r] = chv[r];
-                }
-            }
-            if (xcol) {
-#pragma unroll
-                for (int r = 0; r < R; r++) {
-                    pendH[r] = aRx[r];
-                    pendHU[r] = auRx[r];
+                for (int q = 0; q < NP; q++) {
+                    const float bH = q == 0 ? (lane == 0 ? lowRh : pH) : aRy[(q + NP - 1) % NP].y;
+                    const float bHV = q == 0 ? (lane == 0 ? lowRhv : pHV) : auRy[(q + NP - 1) % NP].y;
+                    syH[q] = add2(make_float2(bH, aRy[q].x), aLy[q]);
+                    syHV[q] = add2(make_float2(bHV, auRy[q].x), auLy[q]);
+                    oldHV[q] = chv[q];
                 }
             }
 #pragma unroll
-            for (int r = 0; r < R; r++) prevX[r] = cx[r];
+            for (int q = 0; q < NP; q++) {
+                if (XCOL) {
+                    pendH[q] = aRx[q];
+                    pendHU[q] = auRx[q];
+                }
+                px[q] = cx[q];
+            }
+            return true;
+        };
+
+        bool ok = column(0, F_{}, F_{}, F_{}, F_{}) && column(1, T_{}, T_{}, F_{}, F_{});
+        if (ok && XC >= 2) {
+            ok = column(2, T_{}, T_{}, T_{}, T_{});
+            for (int k = 3; ok && k <= XC; ++k) ok = column(k, T_{}, T_{}, T_{}, F_{});
         }
+        if (ok) ok = column(XC + 1, T_{}, F_{}, T_{}, T_{});
+        if (!EDGES) smax = fmaxf(smax, hmax >= kDryTol ? wmax : 0.f);
+        const bool bad = !(fabsf(hsum.x + hsum.y) <= FLT_MAX);
         __syncthreads();  // every warp's sweep is done: its stores are visible to the CTA
         if (sAbort) {
             // a copy did not arrive in time: wait (bounded) for the copies in
             // flight, flag the group and leave the kernel
             if (t == 0) {
-                for (int s = 0; s < kRing; s++) mbarWait(smemAddr(&mbar[s]), (phases >> s) & 1u);
+                for (int s = 0; s < kRing; s++) mbarWait(smemAddr(&mbar[s]), (s < slot ? rnd + 1u : rnd) & 1u);
                 atomicOr(&G->status, 4);
             }
             return;
@@ -820,32 +988,35 @@ __global__ void __launch_bounds__(kMaxTileRows / R, MINB) fastStepKernel(const F
     }
 }
 
-/// rows per thread of the step kernel and its resident CTAs per SM (two
-/// rows: the second row's edges give each thread two independent chains;
-/// four CTAs of 128 threads keep the loop free of spills)
-constexpr int kRows = 2;
+/// Packed row pairs per thread of the step kernel and its resident CTAs per
+/// SM.  One pair at four CTAs of 128 threads: 128 registers, no spills, 16
+/// warps per SM.  The kernel is latency-bound, so warps count for more than
+/// instructions: two pairs issue 25% fewer instructions but need 216
+/// registers (8 warps per SM) and run 6% slower; one pair at five CTAs
+/// spills.
+constexpr int kPairs = 1;
 constexpr int kMinCtas = 4;
 
-int fastRows() { return kRows; }
+int fastRows() { return 2 * kPairs; }
 
 cudaError_t launchFastStep(const FastDev &f, int solver, int grid, int tileRows, cudaStream_t s) {
-    const int threads = tileRows / kRows;
+    const int threads = tileRows / (2 * kPairs);
     const cudaError_t e =
         solver == SOLVER_FWAVE
-            ? launchPdlSmem(fastStepKernel<SOLVER_FWAVE, kRows, kMinCtas>, dim3(grid), dim3(threads), kRingBytes, s, f)
-            : launchPdlSmem(fastStepKernel<SOLVER_HLLE, kRows, kMinCtas>, dim3(grid), dim3(threads), kRingBytes, s, f);
+            ? launchPdlSmem(fastStepKernel<SOLVER_FWAVE, kPairs, kMinCtas>, dim3(grid), dim3(threads), kRingBytes, s, f)
+            : launchPdlSmem(fastStepKernel<SOLVER_HLLE, kPairs, kMinCtas>, dim3(grid), dim3(threads), kRingBytes, s, f);
     if (e != cudaSuccess) return e;
     return cudaGetLastError();
 }
 
 int fastOccupancy(int solver, int tileRows) {
     int a = 0;
-    const int threads = tileRows / kRows;
+    const int threads = tileRows / (2 * kPairs);
     if (solver == SOLVER_FWAVE)
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, fastStepKernel<SOLVER_FWAVE, kRows, kMinCtas>, threads,
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, fastStepKernel<SOLVER_FWAVE, kPairs, kMinCtas>, threads,
                                                       kRingBytes);
     else
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, fastStepKernel<SOLVER_HLLE, kRows, kMinCtas>, threads,
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, fastStepKernel<SOLVER_HLLE, kPairs, kMinCtas>, threads,
                                                       kRingBytes);
     return a;
 }
