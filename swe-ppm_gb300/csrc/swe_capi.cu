@@ -275,6 +275,8 @@ struct swe_gpu_domain {
     bool lts = false;
     LtsBlock *dLts = nullptr;
     LtsControl *dLtsCtl = nullptr;
+    int *dLtsWork = nullptr;     // work lists of the running iteration
+    float *dLtsLocal = nullptr;  // published total local time per block
     float *dRing[3] = {nullptr, nullptr, nullptr};
     long long ringElems = 0;
     cudaGraphExec_t ltsGraph = nullptr;
@@ -442,18 +444,15 @@ int enqueueStep(swe_gpu_domain *D) {
     return enqueueUpdate(D);
 }
 
-/// one inner iteration of local time stepping (see swe_lts.cu)
+/// one inner iteration of local time stepping (see swe_lts.cu): check
+/// (with the exchange), speed pass of the blocks at an interval start,
+/// update pass of the enabled blocks (with the iteration's end)
 int enqueueLtsIteration(swe_gpu_domain *D) {
-    CUDA_TRY(launchLtsExchange(D->dev, D->maxPerimeter, D->stream));
     CUDA_TRY(launchLtsCheck(D->dev, D->stream));
-    D->launches += 2;
+    D->launches++;
     int rc = enqueueSpeed(D);
     if (rc) return rc;
-    rc = enqueueUpdate(D);
-    if (rc) return rc;
-    CUDA_TRY(launchLtsDone(D->dev, D->stream));
-    D->launches++;
-    return SWE_GPU_OK;
+    return enqueueUpdate(D);
 }
 
 int readGroups(swe_gpu_domain *D, std::vector<GroupState> &g) {
@@ -475,6 +474,8 @@ void freeDomain(swe_gpu_domain *D) {
     if (D->ltsGraph) cudaGraphExecDestroy(D->ltsGraph);
     cudaFree(D->dLts);
     cudaFree(D->dLtsCtl);
+    cudaFree(D->dLtsWork);
+    cudaFree(D->dLtsLocal);
     for (int f = 0; f < 3; f++) cudaFree(D->dRing[f]);
     if (D->snapEvent) cudaEventDestroy(D->snapEvent);
     for (int i = 0; i < 2; i++) {
@@ -898,6 +899,8 @@ int buildDomain(const std::vector<BlockSpec> &spec, const DomainOptions &o, swe_
     if (D->lts) {
         ok = ok && cudaMalloc(&D->dLts, sizeof(LtsBlock) * D->blocks.size()) == cudaSuccess;
         ok = ok && cudaMalloc(&D->dLtsCtl, sizeof(LtsControl)) == cudaSuccess;
+        ok = ok && cudaMalloc(&D->dLtsWork, sizeof(int) * ltsWorkInts(int(D->blocks.size()))) == cudaSuccess;
+        ok = ok && cudaMalloc(&D->dLtsLocal, sizeof(float) * D->blocks.size()) == cudaSuccess;
         for (int f = 0; f < 3 && ok; f++)
             ok = cudaMalloc(&D->dRing[f], sizeof(float) * std::max(1LL, D->ringElems)) == cudaSuccess;
     }
@@ -949,6 +952,9 @@ int buildDomain(const std::vector<BlockSpec> &spec, const DomainOptions &o, swe_
         cudaMemcpyAsync(D->dLtsCtl, &ctlInit, sizeof(LtsControl), cudaMemcpyHostToDevice, D->stream);
         for (int f = 0; f < 3; f++)
             cudaMemsetAsync(D->dRing[f], 0, sizeof(float) * std::max(1LL, D->ringElems), D->stream);
+        // empty work lists, every block at local time 0
+        cudaMemsetAsync(D->dLtsWork, 0, sizeof(int) * ltsWorkInts(int(D->blocks.size())), D->stream);
+        cudaMemsetAsync(D->dLtsLocal, 0, sizeof(float) * D->blocks.size(), D->stream);
     }
     if (D->bounded) {
         cudaMemcpyAsync(D->dTiles, D->tiles.data(), sizeof(TileInfo) * D->tiles.size(), cudaMemcpyHostToDevice,
@@ -985,6 +991,8 @@ int buildDomain(const std::vector<BlockSpec> &spec, const DomainOptions &o, swe_
     D->dev.tileRows = D->tileRows;
     D->dev.lts = D->dLts;
     D->dev.ltsCtl = D->dLtsCtl;
+    D->dev.ltsWork = D->dLtsWork;
+    D->dev.ltsLocal = D->dLtsLocal;
     for (int f = 0; f < 3; f++) D->dev.ring[f] = D->dRing[f];
     D->dev.tileW = D->dTileW;
     D->dev.tileKey = D->dTileKey;

@@ -163,7 +163,24 @@ struct DomainDev {
     LtsBlock *lts;
     LtsControl *ltsCtl;
     float *ring[3];                  // receive rings of h, hu, hv
+    int *ltsWork;                    // the iteration's work lists (layout: kLw* below)
+    float *ltsLocal;                 // every block's total local time at the end of the last iteration
 };
+
+// Work lists of a local-time-stepping iteration (DomainDev::ltsWork, ints),
+// built by the last CTA of the check kernel: the enabled blocks (update pass)
+// and the enabled blocks at the start of their interval (speed pass), each
+// with the prefix sums of their (row tile, column) pairs, over which the
+// pass's CTAs split the work evenly.  Arrival counters of the check and the
+// update kernel in front.
+constexpr int kLwArrCheck = 0, kLwArrUpd = 1, kLwNUpd = 2, kLwTotUpd = 3, kLwNSpd = 4, kLwTotSpd = 5, kLwHead = 8;
+__host__ __device__ constexpr int ltsWorkInts(int nblocks) { return kLwHead + 4 * nblocks + 2; }
+__host__ __device__ inline int *lwList(int *w, int nblocks, bool update) {
+    return w + kLwHead + (update ? 0 : 2 * nblocks + 1);
+}
+__host__ __device__ inline int *lwPrefix(int *w, int nblocks, bool update) {
+    return lwList(w, nblocks, update) + nblocks;
+}
 
 __device__ __forceinline__ float vmin(float a, float b) { return (b < a) ? b : a; }
 __device__ __forceinline__ float vmax(float a, float b) { return (a < b) ? b : a; }

@@ -57,9 +57,7 @@ int occupancyBound(int solver);
 
 // local time stepping: exchange, ghost-layer check and interval end of one
 // inner iteration (swe_lts.cu)
-cudaError_t launchLtsExchange(const DomainDev &d, int maxPerimeter, cudaStream_t s);
 cudaError_t launchLtsCheck(const DomainDev &d, cudaStream_t s);
-cudaError_t launchLtsDone(const DomainDev &d, cudaStream_t s);
 // getRoundTimestep of the speed pass for a device array of time steps
 cudaError_t launchLtsRound(const float *t, int n, float tsync, int maxDivisor, int *stepSize, cudaStream_t s);
 

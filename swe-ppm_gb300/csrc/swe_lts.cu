@@ -2,21 +2,30 @@
 // and interval bookkeeping of SWE_Block (src/blocks/SWE_Block.hh:311-562) and
 // the overdecomposed driver's inner loop (src/examples/swe_mpi_overdecomp.cpp:266-343).
 //
-// Every block is its own dt group.  One inner iteration is five launches, all
-// decided on the device so that iterations can be replayed from a graph:
-//   ltsExchangeKernel  boundary conditions of every block and, for each side
-//                      connected to a neighbour that is receivable, the
-//                      neighbour's copy layer into the block's receive ring and
-//                      the neighbour's total local time (exchangeGhosts)
-//   ltsCheckKernel     checkAllGhostlayers: copy (same time) or time-interpolate
-//                      (neighbour ahead) each received layer into the ghost
-//                      ring, ghost-layer states, last-timestep notice, step
-//                      counter; the block steps this iteration iff its layers
-//                      are in sync (GroupState::enabled)
-//   speed pass         per block; maxTimestep rounded to Tsync / 2^k
-//   update pass        per enabled block (ghost ring carried into the new buffer)
-//   ltsDoneKernel      every block at its interval end: t += Tsync, counters reset
-// Once t reaches the target the kernels return at once, so a batch of
+// Every block is its own dt group.  One inner iteration is three launches,
+// all decided on the device so that iterations can be replayed from a graph:
+//   ltsCheckKernel  one CTA per block: boundary conditions of the block and,
+//                   for each side connected to a neighbour that is
+//                   receivable, the neighbour's copy layer into the block's
+//                   receive ring with the neighbour's total local time
+//                   (exchangeGhosts); then checkAllGhostlayers: copy (same
+//                   time) or time-interpolate (neighbour ahead) each received
+//                   layer into the ghost ring, ghost-layer states,
+//                   last-timestep notice, step counter.  The block steps this
+//                   iteration iff its layers are in sync (GroupState::enabled).
+//                   The kernel's last CTA lists the enabled blocks and those
+//                   at the start of their interval (DomainDev::ltsWork), and
+//                   gives the others their step Tsync / stepSize.
+//   speed pass      the blocks at the start of an interval: maxTimestep
+//                   rounded to Tsync / 2^k (within an interval the step does
+//                   not depend on the wave speed)
+//   update pass     the enabled blocks (ghost ring carried into the new
+//                   buffer); its last CTA ends the iteration: every block at
+//                   its interval end means t += Tsync, counters reset, and
+//                   every block's total local time is published for the next
+//                   exchange (neighbours read it while their own check runs)
+// Both passes split their list's (row tile, column) pairs evenly over the
+// grid.  Once t reaches the target the kernels do nothing, so a batch of
 // iterations can be queued ahead of the checkpoint.
 #include <cfloat>
 
@@ -27,17 +36,12 @@ namespace swegb {
 
 namespace {
 
-__device__ __forceinline__ bool ltsRunning(const LtsControl &C) { return C.t < C.target && C.iterations < C.iterLimit; }
+constexpr int kLtsCheckThreads = 1024;  // one perimeter position per thread for blocks up to 254 x 254
 
 __device__ __forceinline__ bool ltsReceivable(const LtsBlock &L, int side) {
     if (L.notified) return false;
     const int s = L.received[side];
     return s == GL_NEXT || s == GL_UNVALID || s == GL_SYNC;
-}
-
-__device__ __forceinline__ bool ltsInSync(const LtsBlock &L) {
-    return L.received[0] != GL_UNVALID && L.received[1] != GL_UNVALID && L.received[2] != GL_UNVALID &&
-           L.received[3] != GL_UNVALID && L.stepSizeCounter <= L.stepSize;
 }
 
 /// ghost position p of side `side` (LEFT / RIGHT: rows 1..ny, BOTTOM / TOP:
@@ -73,171 +77,203 @@ __device__ __forceinline__ bool perimeterIndex(const BlockDesc &B, int i, int &s
     return true;
 }
 
-/// applyBoundaryConditions of every block (src/blocks/SWE_Block.hh:757-911)
-/// and the receive half of exchangeGhosts
-/// (src/blocks/SWE_DimensionalSplittingMPIOverdecomp.cpp:273-304 with
-/// local time stepping): grid (perimeter chunks, blocks)
-__global__ void ltsExchangeKernel(const DomainDev d) {
-    pdlWaitAndRelease();
-    const LtsControl C = *d.ltsCtl;
-    if (!ltsRunning(C)) return;
-    const int k = blockIdx.y;
-    const BlockDesc B = d.blocks[k];
-    const int cur = d.groups[k].cur;
-    float *F[3] = {pick(d.h, cur) + B.base, pick(d.hu, cur) + B.base, pick(d.hv, cur) + B.base};
-    const size_t P = size_t(B.pitch);
-    int side, pos;
-    if (!perimeterIndex(B, blockIdx.x * blockDim.x + threadIdx.x, side, pos)) return;
-    if (side == 4) {  // corners from the diagonal interior cell
-        const int gx = (pos & 1) ? B.nx + 1 : 0, gy = (pos & 2) ? B.ny + 1 : 0;
-        const int sx = (pos & 1) ? B.nx : 1, sy = (pos & 2) ? B.ny : 1;
-        for (int f = 0; f < 3; f++) F[f][size_t(gx) * P + gy] = F[f][size_t(sx) * P + sy];
-        return;
-    }
-    int gx, gy, sx, sy;
-    ghostCell(B, side, pos, gx, gy, sx, sy);
-    const int type = B.bnd[side];
-    if (type == WALL || type == OUTFLOW) {
-        const int negate = (type == WALL) ? (side < 2 ? 1 : 2) : -1;  // hu or hv of a wall, nothing for outflow
-        for (int f = 0; f < 3; f++) {
-            const float v = F[f][size_t(sx) * P + sy];
-            F[f][size_t(gx) * P + gy] = (negate == f) ? -v : v;
-        }
-    } else if (type == CONNECT_WITHIN_RANK) {
-        LtsBlock &L = d.lts[k];
-        if (!ltsReceivable(L, side)) return;
-        const int n = B.nbr[side];
-        const BlockDesc N = d.blocks[n];
-        const int ncur = d.groups[n].cur;
-        int nx = sx, ny = sy;  // the neighbour's copy layer
-        switch (side) {
-        case 0: nx = N.nx; break;
-        case 1: nx = 1; break;
-        case 2: ny = N.ny; break;
-        default: ny = 1; break;
-        }
-        const size_t o = size_t(N.base) + size_t(nx) * size_t(N.pitch) + size_t(ny);
-        const long long r = ringOffset(B, side, pos);
-        d.ring[0][r] = pick(d.h, ncur)[o];
-        d.ring[1][r] = pick(d.hu, ncur)[o];
-        d.ring[2][r] = pick(d.hv, ncur)[o];
-        if (pos == 1) L.borderTimestep[side] = ltsTotalLocal(d.lts[n], C);
-    }
-}
-
-/// checkAllGhostlayers (src/blocks/SWE_Block.hh:375-436): one CTA per block
+/// exchangeGhosts + checkAllGhostlayers (src/blocks/SWE_Block.hh:375-436):
+/// one CTA per block; the last CTA lists the iteration's work
 __global__ void ltsCheckKernel(const DomainDev d) {
-    __shared__ int sAction[4];  // 0 none, 1 copy, 2 interpolate
-    __shared__ float sFactor;
+    __shared__ int sAction[4], sRecv[4];  // per side: 0 none, 1 copy, 2 interpolate; layer received now
+    __shared__ float sFactor[4];
+    __shared__ int sLast;
+    __shared__ int sScan[4][kLtsCheckThreads];
     pdlWaitAndRelease();
     const int k = blockIdx.x;
     GroupState *G = d.groups + k;
     const LtsControl C = *d.ltsCtl;
-    if (!ltsRunning(C)) {
-        if (threadIdx.x == 0) G->enabled = 0;
-        return;
-    }
-    const BlockDesc B = d.blocks[k];
-    LtsBlock &L = d.lts[k];
-    const float local = ltsTotalLocal(L, C);
-    if (threadIdx.x == 0) {
-        for (int s = 0; s < 4; s++) sAction[s] = 0;
-        sFactor = 0.f;
-    }
-    __syncthreads();
-    if (threadIdx.x < 4) {
-        const int s = threadIdx.x;
-        const int type = B.bnd[s];
-        if (type == CONNECT || type == CONNECT_WITHIN_RANK) {
-            const float bt = L.borderTimestep[s];
-            if (fabs(double(bt - local)) <= DBL_EPSILON) sAction[s] = 1;
-            else if (bt > local) sAction[s] = 2;
-        }
-    }
-    __syncthreads();
-    // the received layers into the ghost ring of the current buffer
-    const int cur = G->cur;
-    float *F[3] = {pick(d.h, cur) + B.base, pick(d.hu, cur) + B.base, pick(d.hv, cur) + B.base};
-    const size_t P = size_t(B.pitch);
-    for (int i = threadIdx.x; i < 2 * B.ny + 2 * B.nx; i += blockDim.x) {
-        int side, pos;
-        perimeterIndex(B, i, side, pos);
-        const int a = sAction[side];
-        if (!a) continue;
-        int gx, gy, sx, sy;
-        ghostCell(B, side, pos, gx, gy, sx, sy);
-        const long long r = ringOffset(B, side, pos);
-        // interpolateValue: old + (new - old) * (local / remote)
-        const float factor = a == 2 ? local / L.borderTimestep[side] : 0.f;
-        for (int f = 0; f < 3; f++) {
-            float &g = F[f][size_t(gx) * P + gy];
-            const float nv = d.ring[f][r];
-            g = (a == 1) ? nv : g + (nv - g) * factor;
-        }
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        for (int s = 0; s < 4; s++) {
+    const bool running = ltsRunning(C);
+    if (running) {
+        const BlockDesc &B = d.blocks[k];
+        LtsBlock &L = d.lts[k];
+        const float local = ltsTotalLocal(L, C);
+        // per side: whether the neighbour's layer is received now (with the
+        // neighbour's total local time, published at the end of the last
+        // iteration; its own check runs at the same time), the border time
+        // after that, and what checkAllGhostlayers does with the layer: copy
+        // (same time) or interpolate (neighbour ahead)
+        if (threadIdx.x < 4) {
+            const int s = threadIdx.x;
             const int type = B.bnd[s];
-            if (type != CONNECT && type != CONNECT_WITHIN_RANK) continue;
-            const float bt = L.borderTimestep[s];
-            L.received[s] = sAction[s] == 1 ? GL_SYNC : sAction[s] == 2 ? GL_INTER : GL_UNVALID;
-            if (bt >= C.duration) L.received[s] = GL_DONE;
+            int recv = 0, a = 0;
+            float bt = L.borderTimestep[s];
+            if (type == CONNECT_WITHIN_RANK && ltsReceivable(L, s)) {
+                recv = 1;
+                bt = __ldcg(&d.ltsLocal[B.nbr[s]]);
+                L.borderTimestep[s] = bt;
+            }
+            if (type == CONNECT || type == CONNECT_WITHIN_RANK) {
+                if (fabs(double(bt - local)) <= DBL_EPSILON) a = 1;
+                else if (bt > local) a = 2;
+            }
+            sRecv[s] = recv;
+            sAction[s] = a;
+            sFactor[s] = a == 2 ? local / bt : 0.f;  // interpolateValue: old + (new - old) * (local / remote)
         }
-        if (fabs(double(C.duration - local)) <= DBL_EPSILON || local >= C.duration) L.notified = 1;
-        if (ltsInSync(L)) {
-            for (int s = 0; s < 4; s++)
-                if (L.received[s] != GL_DONE) L.received[s] = (L.received[s] == GL_INTER) ? GL_INTER : GL_NEXT;
+        __syncthreads();
+        // one pass over the perimeter: boundary conditions and corners
+        // (applyBoundaryConditions, src/blocks/SWE_Block.hh:757-911), the
+        // received layer into the receive ring (exchangeGhosts,
+        // src/blocks/SWE_DimensionalSplittingMPIOverdecomp.cpp:273-304), the
+        // ring into the ghost ring of the current buffer
+        const int cur = G->cur;
+        float *F[3] = {pick(d.h, cur) + B.base, pick(d.hu, cur) + B.base, pick(d.hv, cur) + B.base};
+        const size_t P = size_t(B.pitch);
+        for (int i = threadIdx.x; i < 2 * B.ny + 2 * B.nx + 4; i += blockDim.x) {
+            int side, pos;
+            perimeterIndex(B, i, side, pos);
+            if (side == 4) {  // corners from the diagonal interior cell
+                const int gx = (pos & 1) ? B.nx + 1 : 0, gy = (pos & 2) ? B.ny + 1 : 0;
+                const int sx = (pos & 1) ? B.nx : 1, sy = (pos & 2) ? B.ny : 1;
+                for (int f = 0; f < 3; f++) F[f][size_t(gx) * P + gy] = F[f][size_t(sx) * P + sy];
+                continue;
+            }
+            int gx, gy, sx, sy;
+            ghostCell(B, side, pos, gx, gy, sx, sy);
+            const int type = B.bnd[side];
+            if (type == WALL || type == OUTFLOW) {
+                const int negate = (type == WALL) ? (side < 2 ? 1 : 2) : -1;  // hu or hv of a wall, nothing for outflow
+                for (int f = 0; f < 3; f++) {
+                    const float v = F[f][size_t(sx) * P + sy];
+                    F[f][size_t(gx) * P + gy] = (negate == f) ? -v : v;
+                }
+                continue;
+            }
+            const long long r = ringOffset(B, side, pos);
+            float v[3];
+            if (sRecv[side]) {
+                const int n = B.nbr[side];
+                const BlockDesc &N = d.blocks[n];
+                const int ncur = d.groups[n].cur;
+                int nx = sx, ny = sy;  // the neighbour's copy layer
+                switch (side) {
+                case 0: nx = N.nx; break;
+                case 1: nx = 1; break;
+                case 2: ny = N.ny; break;
+                default: ny = 1; break;
+                }
+                const size_t o = size_t(N.base) + size_t(nx) * size_t(N.pitch) + size_t(ny);
+                v[0] = pick(d.h, ncur)[o];
+                v[1] = pick(d.hu, ncur)[o];
+                v[2] = pick(d.hv, ncur)[o];
+                for (int f = 0; f < 3; f++) d.ring[f][r] = v[f];
+            }
+            const int a = sAction[side];
+            if (!a) continue;
+            if (!sRecv[side])
+                for (int f = 0; f < 3; f++) v[f] = d.ring[f][r];
+            const float factor = sFactor[side];
+            for (int f = 0; f < 3; f++) {
+                float &g = F[f][size_t(gx) * P + gy];
+                g = (a == 1) ? v[f] : g + (v[f] - g) * factor;
+            }
         }
-        if (ltsInSync(L) && L.stepSizeCounter < L.stepSize) L.stepSizeCounter++;
-        G->enabled = ltsInSync(L) ? 1 : 0;  // read by the next kernels, after this grid ends
-    }
-}
-
-/// end of an inner iteration: once every block has reached its interval end
-/// (hasMaxLocalTimestep, src/blocks/SWE_Block.hh:311-367) the interval is
-/// done: t += Tsync, counters reset (src/examples/swe_mpi_overdecomp.cpp:332-342)
-__global__ void ltsDoneKernel(const DomainDev d) {
-    pdlWaitAndRelease();
-    LtsControl &C = *d.ltsCtl;
-    if (!ltsRunning(C)) return;
-    bool done = true;
-    for (int k = threadIdx.x; k < d.nblocks; k += blockDim.x) {
-        const LtsBlock &L = d.lts[k];
-        if (!((L.stepSizeCounter >= L.stepSize && ltsInSync(L)) || L.notified)) done = false;
-    }
-    done = __syncthreads_and(done);
-    if (done) {
-        for (int k = threadIdx.x; k < d.nblocks; k += blockDim.x) {
-            LtsBlock &L = d.lts[k];
-            L.lastStepSize = L.stepSize;
-            L.stepSizeCounter = 0;
-            L.stepSize = 0;
-            L.timestepCounter++;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (int s = 0; s < 4; s++) {
+                const int type = B.bnd[s];
+                if (type != CONNECT && type != CONNECT_WITHIN_RANK) continue;
+                const float bt = L.borderTimestep[s];
+                L.received[s] = sAction[s] == 1 ? GL_SYNC : sAction[s] == 2 ? GL_INTER : GL_UNVALID;
+                if (bt >= C.duration) L.received[s] = GL_DONE;
+            }
+            if (fabs(double(C.duration - local)) <= DBL_EPSILON || local >= C.duration) L.notified = 1;
+            if (ltsInSync(L)) {
+                for (int s = 0; s < 4; s++)
+                    if (L.received[s] != GL_DONE) L.received[s] = (L.received[s] == GL_INTER) ? GL_INTER : GL_NEXT;
+            }
+            if (ltsInSync(L) && L.stepSizeCounter < L.stepSize) L.stepSizeCounter++;
+            G->enabled = ltsInSync(L) ? 1 : 0;
         }
+    } else if (threadIdx.x == 0) {
+        G->enabled = 0;
     }
+    // the last CTA lists the enabled blocks (update pass) and those at the
+    // start of their interval (speed pass); the others take Tsync / stepSize,
+    // the step the speed pass would round to (SWE_Block::getRoundTimestep)
     __syncthreads();
-    if (threadIdx.x == 0) {
-        C.iterations++;
-        if (done) {
-            C.t = C.t + C.maxTimestepLocal;
-            C.intervals++;
+    if (threadIdx.x == 0)
+        sLast = arriveAcqRel(reinterpret_cast<unsigned *>(d.ltsWork + kLwArrCheck), 1u) + 1u == gridDim.x;
+    __syncthreads();
+    if (sLast) {
+        // thread i takes blocks [i c, (i+1) c); exclusive scans of the counts
+        // and pairs over the threads give every entry its place (block order)
+        int *W = d.ltsWork;
+        const int nb = d.nblocks, TY = d.tileRows, T = blockDim.x, i = threadIdx.x;
+        const int chunk = (nb + T - 1) / T;
+        const int j0 = min(nb, i * chunk), j1 = min(nb, j0 + chunk);
+        auto entry = [&](int j, int &pairs, bool &upd, bool &spd) {
+            const BlockDesc &Bj = d.blocks[j];
+            pairs = ((Bj.ny + TY - 1) / TY) * Bj.nx;
+            upd = __ldcg(&d.groups[j].enabled) != 0;
+            spd = upd && __ldcg(&d.lts[j].stepSizeCounter) <= 0;
+        };
+        int v[4] = {0, 0, 0, 0};  // enabled blocks, their pairs, interval starts, their pairs
+        for (int j = j0; j < j1; j++) {
+            int pairs;
+            bool upd, spd;
+            entry(j, pairs, upd, spd);
+            if (upd) {
+                v[0]++;
+                v[1] += pairs;
+            }
+            if (spd) {
+                v[2]++;
+                v[3] += pairs;
+            } else if (upd) {
+                d.groups[j].dt = C.maxTimestepLocal / float(__ldcg(&d.lts[j].stepSize));
+            }
+        }
+        for (int q = 0; q < 4; q++) sScan[q][i] = v[q];
+        __syncthreads();
+        for (int off = 1; off < T; off *= 2) {  // inclusive scans (Hillis-Steele)
+            int w[4];
+            for (int q = 0; q < 4; q++) w[q] = i >= off ? sScan[q][i - off] : 0;
+            __syncthreads();
+            for (int q = 0; q < 4; q++) sScan[q][i] += w[q];
+            __syncthreads();
+        }
+        int o[4];
+        for (int q = 0; q < 4; q++) o[q] = sScan[q][i] - v[q];
+        int *lU = lwList(W, nb, true), *pU = lwPrefix(W, nb, true);
+        int *lS = lwList(W, nb, false), *pS = lwPrefix(W, nb, false);
+        for (int j = j0; j < j1; j++) {
+            int pairs;
+            bool upd, spd;
+            entry(j, pairs, upd, spd);
+            if (upd) {
+                pU[o[0]] = o[1];
+                lU[o[0]++] = j;
+                o[1] += pairs;
+            }
+            if (spd) {
+                pS[o[2]] = o[3];
+                lS[o[2]++] = j;
+                o[3] += pairs;
+            }
+        }
+        if (i == T - 1) {
+            W[kLwNUpd] = o[0];
+            W[kLwTotUpd] = o[1];
+            W[kLwNSpd] = o[2];
+            W[kLwTotSpd] = o[3];
+            pU[o[0]] = o[1];
+            pS[o[2]] = o[3];
+            W[kLwArrCheck] = 0;
         }
     }
 }
 
 } // namespace
 
-cudaError_t launchLtsExchange(const DomainDev &d, int maxPerimeter, cudaStream_t s) {
-    const int threads = 128;
-    return launchPdl(ltsExchangeKernel, dim3((maxPerimeter + 4 + threads - 1) / threads, unsigned(d.nblocks)),
-                     dim3(threads), s, d);
-}
 cudaError_t launchLtsCheck(const DomainDev &d, cudaStream_t s) {
-    return launchPdl(ltsCheckKernel, dim3(unsigned(d.nblocks)), dim3(256), s, d);
-}
-cudaError_t launchLtsDone(const DomainDev &d, cudaStream_t s) {
-    return launchPdl(ltsDoneKernel, dim3(1), dim3(256), s, d);
+    return launchPdl(ltsCheckKernel, dim3(unsigned(d.nblocks)), dim3(kLtsCheckThreads), s, d);
 }
 
 /// getRoundTimestep of a block at the start of an interval for every entry

@@ -145,19 +145,101 @@ template <int S> __device__ __forceinline__ void cellQuantities(float h, float h
     cy = makeCell(h, hv, b, uy, sq, c);
 }
 
+__device__ __forceinline__ bool ltsRunning(const LtsControl &C) { return C.t < C.target && C.iterations < C.iterLimit; }
+
+__device__ __forceinline__ bool ltsInSync(const LtsBlock &L) {
+    return L.received[0] != GL_UNVALID && L.received[1] != GL_UNVALID && L.received[2] != GL_UNVALID &&
+           L.received[3] != GL_UNVALID && L.stepSizeCounter <= L.stepSize;
+}
+
+/// Segments of this CTA under local time stepping: the pass's work list
+/// (DomainDev::ltsWork) names the blocks that take part, with the prefix sums
+/// of their (row tile, column) pairs; CTA c takes pairs [total c / grid,
+/// total (c+1) / grid), cut at tile ends and every kMaxTileCols columns.
+/// segment(unit, pairs, block's pairs) runs each piece.
+template <bool UPDATE, class Seg>
+__device__ __forceinline__ void ltsSegments(const DomainDev &d, int TY, Seg &&segment) {
+    int *W = d.ltsWork;
+    const int n = __ldcg(W + (UPDATE ? kLwNUpd : kLwNSpd));
+    const long long total = __ldcg(W + (UPDATE ? kLwTotUpd : kLwTotSpd));
+    const int *list = lwList(W, d.nblocks, UPDATE);
+    const int *pref = lwPrefix(W, d.nblocks, UPDATE);
+    long long pos = total * blockIdx.x / gridDim.x;
+    const long long end = total * (blockIdx.x + 1) / gridDim.x;
+    if (pos >= end || n <= 0) return;
+    int lo = 0, hi = n - 1;  // the entry holding pair pos: pref[j] <= pos < pref[j+1]
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) / 2;
+        if (__ldcg(pref + mid) <= pos) lo = mid;
+        else hi = mid - 1;
+    }
+    int j = lo;
+    while (pos < end) {
+        const int k = __ldcg(list + j);
+        const BlockDesc &B = d.blocks[k];
+        const long long local = pos - __ldcg(pref + j);
+        const int nx = B.nx;
+        const int tile = int(local / nx), col = int(local % nx) + 1;
+        const int len = int(min((long long)min(nx + 1 - col, kMaxTileCols), end - pos));
+        const int tiles = (B.ny + TY - 1) / TY;
+        segment(WorkUnit{k, 1 + tile * TY, col, col + len}, unsigned(len), unsigned(tiles * nx));
+        pos += len;
+        if (pos >= __ldcg(pref + j + 1)) ++j;
+    }
+}
+
+/// End of a local-time-stepping iteration, run by one CTA (the update pass's
+/// last): once every block has reached its interval end (hasMaxLocalTimestep,
+/// src/blocks/SWE_Block.hh:311-367) the interval is done: t += Tsync,
+/// counters reset (src/examples/swe_mpi_overdecomp.cpp:332-342).  Every
+/// block's total local time is published for the next iteration's exchange.
+__device__ __forceinline__ void ltsEndIteration(const DomainDev &d) {
+    LtsControl &C = *d.ltsCtl;
+    const bool running = ltsRunning(C);
+    bool done = true;
+    if (running)
+        for (int k = threadIdx.x; k < d.nblocks; k += blockDim.x) {
+            const LtsBlock &L = d.lts[k];
+            if (!((L.stepSizeCounter >= L.stepSize && ltsInSync(L)) || L.notified)) done = false;
+        }
+    done = __syncthreads_and(done);
+    if (running && done) {
+        for (int k = threadIdx.x; k < d.nblocks; k += blockDim.x) {
+            LtsBlock &L = d.lts[k];
+            L.lastStepSize = L.stepSize;
+            L.stepSizeCounter = 0;
+            L.stepSize = 0;
+            L.timestepCounter++;
+        }
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < d.nblocks; k += blockDim.x) d.ltsLocal[k] = ltsTotalLocal(d.lts[k], C);
+    if (threadIdx.x == 0 && running) {
+        C.iterations++;
+        if (done) {
+            C.t = C.t + C.maxTimestepLocal;
+            C.intervals++;
+        }
+    }
+}
+
 /// the segment's share of the running pass is done; the last segment of the
 /// group finishes the pass (dt after the speed pass; clock, step count and
 /// current buffer after the update pass)
+///
+/// A segment adds `count` to the group's arrivals; the pass is complete at
+/// `total` (0: the group's segment count of the static partition).
 template <bool UPDATE>
 __device__ __forceinline__ void segmentDone(const DomainDev &d, GroupState *G, float segMax, float *sRed, int *sLast,
-                                            int cur) {
+                                            int cur, unsigned count = 1u, unsigned total = 0u) {
     float m = 0.f;
     if (!UPDATE) m = blockReduceMax(segMax, sRed);
     __syncthreads();
     if (threadIdx.x == 0) {
         if (!UPDATE) atomicMax(&G->speedBits, __float_as_uint(m));
-        const unsigned prev = arriveAcqRel(&G->arrived, 1u);
-        *sLast = (prev == unsigned(UPDATE ? G->unitsUpd : G->units) - 1u);
+        const unsigned prev = arriveAcqRel(&G->arrived, count);
+        const unsigned need = total ? total : unsigned(UPDATE ? G->unitsUpd : G->units);
+        *sLast = (prev + count == need);
     }
     __syncthreads();
     // the group state the last segment writes is read by the next kernel,
@@ -334,12 +416,13 @@ __global__ void __launch_bounds__(kMaxTileRows, 4) sweepKernel(const DomainDev d
     __shared__ float sRed[kMaxTileRows / 32];
     __shared__ int sLast;
     const bool bounds = BOUNDS && d.tileW != nullptr;
-    // the partition and the block descriptors are written only when the domain
-    // is built: bring the first segment's into L1 before waiting for the
+    // the static partition and the block descriptors are written only when
+    // the domain is built (local time stepping's work lists are not: they
+    // come from the previous kernel): bring the first segment's into L1 before waiting for the
     // previous kernel.  The update pass also prefetches the segment's first
     // columns into L2 from the buffer the group state names now (a hint only:
     // every value used is loaded after the wait).
-    {
+    if (!d.ltsWork) {
         const int s0 = d.ctaSeg[blockIdx.x];
         if (s0 < d.ctaSeg[blockIdx.x + 1]) {
             const WorkUnit w0 = d.units[s0];
@@ -374,12 +457,11 @@ __global__ void __launch_bounds__(kMaxTileRows, 4) sweepKernel(const DomainDev d
     pdlWaitAndRelease();
 
     const int t = threadIdx.x, TY = blockDim.x;
-    const int segEnd = d.ctaSeg[blockIdx.x + 1];
-    for (int seg = d.ctaSeg[blockIdx.x]; seg < segEnd; ++seg) {
-        const WorkUnit wu = d.units[seg];
+    // one segment: rows [wu.y0, wu.y0 + TY) x columns [wu.x0, wu.x1) of a block
+    auto segment = [&](const WorkUnit wu, unsigned count, unsigned total) {
         const BlockDesc B = d.blocks[wu.block];
         GroupState *G = d.groups + B.group;
-        if (!groupActive(G)) continue;
+        if (!groupActive(G)) return;
         const int cur = __ldg(&G->cur);
         const float *__restrict__ H = pick(d.h, cur) + B.base;
         const float *__restrict__ HU = pick(d.hu, cur) + B.base;
@@ -585,7 +667,24 @@ __global__ void __launch_bounds__(kMaxTileRows, 4) sweepKernel(const DomainDev d
             }
         }
         if (UPDATE && __syncthreads_or(bad) && t == 0) atomicOr(&G->status, 2);
-        segmentDone<UPDATE>(d, G, smax, sRed, &sLast, cur);
+        segmentDone<UPDATE>(d, G, smax, sRed, &sLast, cur, count, total);
+    };
+    if (d.ltsWork) {
+        ltsSegments<UPDATE>(d, TY, segment);
+        if (UPDATE) {
+            // the update pass's last CTA ends the iteration
+            __syncthreads();
+            if (t == 0)
+                sLast = arriveAcqRel(reinterpret_cast<unsigned *>(d.ltsWork + kLwArrUpd), 1u) + 1u == gridDim.x;
+            __syncthreads();
+            if (sLast) {
+                if (t == 0) d.ltsWork[kLwArrUpd] = 0;
+                ltsEndIteration(d);
+            }
+        }
+    } else {
+        const int segEnd = d.ctaSeg[blockIdx.x + 1];
+        for (int seg = d.ctaSeg[blockIdx.x]; seg < segEnd; ++seg) segment(d.units[seg], 1u, 0u);
     }
 }
 
