@@ -331,6 +331,36 @@ def reference_run(binary, duration, blocks=N_BLOCKS, cells=N_CELLS_SIDE):
     return flop / 270.0, el
 
 
+def port_tsunami_state():
+    """The tsunami workload's shape for the oracle port, built with numpy
+    alone (the CPU legs load no product library): 2048^2 over 100 km as 4 x 4
+    blocks of 512^2 in the blocks' Float2D layout with ghost rings, sinusoidal
+    bathymetry around -2000 m with seeded noise, still water and a 5 m bump.
+    The cost of a wet step does not depend on the values."""
+    n, nb = N_CELLS_SIDE, 4
+    m = n // nb
+    L = 100000.0
+    dx = L / n
+    rng = np.random.default_rng(SEED)
+    xc = (np.arange(n) + 0.5) * dx
+    X, Y = np.meshgrid(xc, xc, indexing="ij")
+    bath = -2000.0 + 500.0 * np.sin(2 * np.pi * X / L) * np.cos(2 * np.pi * Y / L) + rng.normal(0.0, 20.0, (n, n))
+    cx, cy = rng.uniform(0.3 * L, 0.7 * L, 2)
+    eta = 5.0 * np.exp(-((X - cx) ** 2 + (Y - cy) ** 2) / (2 * 5000.0 ** 2))
+    fields = [eta - bath, np.zeros((n, n)), np.zeros((n, n)), bath]
+    parts = [[], [], [], []]
+    for k in range(nb * nb):
+        px, py = k // nb, k % nb
+        for i, f in enumerate(fields):
+            blk = np.zeros((m + 2, m + 2), np.float32)
+            blk[1:-1, 1:-1] = f[px * m:(px + 1) * m, py * m:(py + 1) * m]
+            blk[0, :], blk[-1, :] = blk[1, :], blk[-2, :]
+            blk[:, 0], blk[:, -1] = blk[:, 1], blk[:, -2]
+            parts[i].append(blk.ravel())
+    geo = dict(dx=dx, dy=dx, nx_cols=[m] * nb, ny_rows=[m] * nb, boundary=[0] * 4)
+    return (geo,) + tuple(np.concatenate(p) for p in parts)
+
+
 def run_reference(args, world, rank):
     """The reference's own CPU path on the host cores: its stock
     overdecomposed driver (swe_benchmark_mpioverdecomp: 16 blocks of 512^2,
@@ -361,10 +391,8 @@ def run_reference(args, world, rank):
         ms_per_step = 1e3 * N_CELLS_SIDE * N_CELLS_SIDE / value
     else:
         import oracle
-        import swe_gb300 as swe
         oracle.build()
-        geo, h, hu, hv, b = swe.init_domain(swe.SCENARIO_TSUNAMI, N_CELLS_SIDE, N_CELLS_SIDE, N_BLOCKS,
-                                            [N_CELLS_SIDE, SEED, 100000.0])
+        geo, h, hu, hv, b = port_tsunami_state()
         R = oracle.Domain(geo["nx_cols"], geo["ny_rows"], geo["dx"], geo["dy"], outer=geo["boundary"],
                           solver=oracle.HLLE)
         R.set_state(h, hu, hv, b)
