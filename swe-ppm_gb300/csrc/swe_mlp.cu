@@ -95,6 +95,8 @@ __device__ __forceinline__ float silu(float z) {
     const float h = 0.5f * z;
     return fmaf(h, tanhApprox(h), h);
 }
+/// the same from h = z / 2
+__device__ __forceinline__ float siluHalf(float h) { return fmaf(h, tanhApprox(h), h); }
 /// d SiLU / dz = s (1 + z (1 - s)), s = sigmoid(z) = (1 + tanh(z / 2)) / 2
 __device__ __forceinline__ float dsilu(float z) {
     const float s = fmaf(0.5f, tanhApprox(0.5f * z), 0.5f);
@@ -218,15 +220,19 @@ __device__ __forceinline__ void store16(uint8_t *s, int row, int c, const uint32
     *reinterpret_cast<uint4 *>(s + tc::coreOffset(row, c + 8, kHid)) = make_uint4(p[4], p[5], p[6], p[7]);
 }
 
-/// epilogue of a hidden layer: A = bf16(silu(Z + b)) for this thread's row
-__device__ __forceinline__ void epilogueSilu(uint32_t tz, const float *bias, uint8_t *dst, int row) {
+/// epilogue of a hidden layer: A = bf16(silu(Z + b)) for this thread's row;
+/// hbias = b / 2, so h = (Z + b) / 2 is one fused multiply-add, rounded as
+/// 0.5 (Z + b)
+__device__ __forceinline__ void epilogueSilu(uint32_t tz, const float *hbias, uint8_t *dst, int row) {
 #pragma unroll
     for (int c = 0; c < kHid; c += 16) {
         float v[16];
         tc::load16(tz, c, v);
         uint32_t p[8];
 #pragma unroll
-        for (int j = 0; j < 8; j++) p[j] = packBf16(silu(v[2 * j] + bias[c + 2 * j]), silu(v[2 * j + 1] + bias[c + 2 * j + 1]));
+        for (int j = 0; j < 8; j++)
+            p[j] = packBf16(siluHalf(fmaf(0.5f, v[2 * j], hbias[c + 2 * j])),
+                            siluHalf(fmaf(0.5f, v[2 * j + 1], hbias[c + 2 * j + 1])));
         store16(dst, row, c, p);
     }
 }
@@ -261,28 +267,31 @@ __device__ __forceinline__ bool awaitMma(uint64_t *mbar, uint32_t &phase) {
     return ok;
 }
 
-/// stage the packed weights (and biases) into shared memory
-__device__ __forceinline__ void stageImage(const uint8_t *image, uint8_t *s) {
+/// stage the packed weights (and biases) into shared memory, and the hidden
+/// layers' halved biases (the SiLU epilogue works on (Z + b) / 2)
+__device__ __forceinline__ void stageImage(const uint8_t *image, uint8_t *s, float *hbias) {
     const int4 *src = reinterpret_cast<const int4 *>(image);
     int4 *dst = reinterpret_cast<int4 *>(s);
     for (int i = threadIdx.x; i < kImageBytes / 16; i += blockDim.x) dst[i] = __ldg(src + i);
+    const float *b = reinterpret_cast<const float *>(image + pBias);
+    for (int i = threadIdx.x; i < 3 * kHid; i += blockDim.x) hbias[i] = 0.5f * __ldg(b + i);
 }
 
 /// the four forward GEMMs of one tile, with the epilogues between them; on
 /// return the raw outputs sit in TMEM columns oCol.. (without b4).  act[l] is
 /// the shared-memory buffer of layer l's output activations, zc[l] the TMEM
 /// columns of its pre-activations.
-__device__ __forceinline__ bool forwardTile(uint32_t tm, const uint8_t *sW, const uint8_t *sX0, uint8_t *const act[3],
-                                            const uint32_t zc[3], uint32_t oCol, uint64_t *mbar, uint32_t &phase) {
+__device__ __forceinline__ bool forwardTile(uint32_t tm, const uint8_t *sW, const float *hbias, const uint8_t *sX0,
+                                            uint8_t *const act[3], const uint32_t zc[3], uint32_t oCol, uint64_t *mbar,
+                                            uint32_t &phase) {
     const int t = threadIdx.x;
-    const float *bias = reinterpret_cast<const float *>(sW + pBias);
     publishToMma();
     if (t == 0) {
         tc::mma(tm + zc[0], tc::smemDesc(sX0, 0, kInPad), tc::smemDesc(sW + pW1, 0, kInPad), tc::idescBf16(128, kHid), false);
         tc::commit(mbar);
     }
     if (!awaitMma(mbar, phase)) return false;
-    epilogueSilu(tm + zc[0], bias, act[0], t);
+    epilogueSilu(tm + zc[0], hbias, act[0], t);
     const int pw[2] = {pW2, pW3};
 #pragma unroll
     for (int l = 0; l < 2; l++) {
@@ -295,7 +304,7 @@ __device__ __forceinline__ bool forwardTile(uint32_t tm, const uint8_t *sW, cons
             tc::commit(mbar);
         }
         if (!awaitMma(mbar, phase)) return false;
-        epilogueSilu(tm + zc[l + 1], bias + kHid * (l + 1), act[l + 1], t);
+        epilogueSilu(tm + zc[l + 1], hbias + kHid * (l + 1), act[l + 1], t);
     }
     publishToMma();
     if (t == 0) {
@@ -328,9 +337,10 @@ __global__ void __launch_bounds__(128) forwardKernel(const uint8_t *image, EdgeB
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ __align__(8) uint64_t mbar;
     __shared__ uint32_t tslot;
+    __shared__ float sHb[3 * kHid];  // halved hidden-layer biases
     const int t = threadIdx.x;
     uint8_t *sW = smem, *sX0 = smem + kFwdX0, *sAct = smem + kFwdAct;
-    stageImage(image, sW);
+    stageImage(image, sW, sHb);
     if (t == 0) tc::mbarInit(&mbar, 1);
     if (t < 32) tc::tmemAlloc(&tslot, kFwdCols);
     tc::fenceBeforeSync();
@@ -356,7 +366,7 @@ __global__ void __launch_bounds__(128) forwardKernel(const uint8_t *image, EdgeB
         EdgeFeat f;
         edgeFeatures(q[0], q[1], q[2], q[3], q[4], q[5], f);
         storeX0(sX0, t, f.x);
-        if (!(ok = forwardTile(tm, sW, sX0, act, zc, 0, &mbar, phase))) break;
+        if (!(ok = forwardTile(tm, sW, sHb, sX0, act, zc, 0, &mbar, phase))) break;
         float v[16];
         tc::load16(tm, 0, v);
         float o[4];
@@ -401,11 +411,12 @@ __global__ void __launch_bounds__(128, 1) trainKernel(const uint8_t *image, Edge
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ __align__(8) uint64_t mbar;
     __shared__ uint32_t tslot;
+    __shared__ float sHb[3 * kHid];  // halved hidden-layer biases
     __shared__ float warpLoss[4];
     const int t = threadIdx.x;
     uint8_t *sW = smem, *sOnes = smem + kTrOnes, *sX0 = smem + kTrX0, *sDZ4 = smem + kTrDZ4, *sDZ = smem + kTrDZ;
     uint8_t *const act[3] = {smem + kTrA1, smem + kTrA2, smem + kTrA3};
-    stageImage(image, sW);
+    stageImage(image, sW, sHb);
     for (int i = t; i < kOnesBytes / 4; i += blockDim.x) reinterpret_cast<uint32_t *>(sOnes)[i] = 0x3F803F80u;  // BF16 1.0
     for (int i = t; i < (kTrEnd - kTrDZ4) / 4; i += blockDim.x) reinterpret_cast<uint32_t *>(sDZ4)[i] = 0u;
     if (t == 0) tc::mbarInit(&mbar, 1);
@@ -434,7 +445,7 @@ __global__ void __launch_bounds__(128, 1) trainKernel(const uint8_t *image, Edge
         EdgeFeat f;
         edgeFeatures(q[0], q[1], q[2], q[3], q[4], q[5], f);
         storeX0(sX0, t, f.x);
-        if (!(ok = forwardTile(tm, sW, sX0, act, zc, cO, &mbar, phase))) break;
+        if (!(ok = forwardTile(tm, sW, sHb, sX0, act, zc, cO, &mbar, phase))) break;
         // loss and dLoss/dO
         {
             float v[16];
@@ -693,12 +704,13 @@ __global__ void __launch_bounds__(128) surrogateEdgeKernel(const DomainDev d, co
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ __align__(8) uint64_t mbar;
     __shared__ uint32_t tslot;
+    __shared__ float sHb[3 * kHid];  // halved hidden-layer biases
     __shared__ float sMax[4];
     const int t = threadIdx.x;
     uint8_t *sW = smem, *sX0 = smem + kFwdX0, *sAct = smem + kFwdAct;
     uint32_t tm = 0;
     if (SURR) {
-        stageImage(image, sW);
+        stageImage(image, sW, sHb);
         if (t == 0) tc::mbarInit(&mbar, 1);
         if (t < 32) tc::tmemAlloc(&tslot, kFwdCols);
         tc::fenceBeforeSync();
@@ -734,7 +746,7 @@ __global__ void __launch_bounds__(128) surrogateEdgeKernel(const DomainDev d, co
             EdgeFeat f;
             edgeFeatures(q[0], q[1], q[2], q[3], q[4], q[5], f);
             storeX0(sX0, t, f.x);
-            if (!(ok = forwardTile(tm, sW, sX0, act, zc, 0, &mbar, phase))) break;
+            if (!(ok = forwardTile(tm, sW, sHb, sX0, act, zc, 0, &mbar, phase))) break;
             float v[16];
             tc::load16(tm, 0, v);
             float o[4];
