@@ -524,6 +524,10 @@ __global__ void __launch_bounds__(kMaxTileRows, 4) sweepKernel(const DomainDev d
             cellQuantities<S>(H[o + 1], HU[o + 1], HV[o + 1], BT[o + 1], dummy, R);
             if (UPDATE) {
                 float aL, aR, auL, auR, s;
+                // edgeSolve<S, true> leaves out the + 0 of the routing's
+                // left-going parts (sTop here, aL/auL below): each is only ever
+                // added to a right-going part, which is never -0, so every
+                // sum keeps the reference's sign of zero
                 edgeSolve<S, true>(L, R, aL, aR, auL, auR, s);
                 if (top) {
                     sTop[0][k] = aL;
