@@ -118,6 +118,8 @@ struct __align__(128) GroupState {
     int prevDir, prevValid;
     int lastCandidates;      // tiles the last bounded speed pass evaluated edge by edge
     int unitsFast;           // segments of the fast-arithmetic step in this group
+    int ringStale;           // local time stepping: the update flipped the buffers; the
+                             // current buffer's ghost ring is still in the other one
 };
 
 // Bound tile of the bounded speed pass: 32 x 32 interior cells of a block,

@@ -89,10 +89,16 @@ __global__ void ltsCheckKernel(const DomainDev d) {
     GroupState *G = d.groups + k;
     const LtsControl C = *d.ltsCtl;
     const bool running = ltsRunning(C);
+    const BlockDesc &B = d.blocks[k];
+    LtsBlock &L = d.lts[k];
+    const int cur = G->cur;
+    // the update pass writes no ghosts: after it the current buffer's ring
+    // (and corners) are still in the other buffer; the reference's single
+    // array keeps them, so they are carried over first
+    const bool stale = G->ringStale != 0;
+    float local = 0.f;
     if (running) {
-        const BlockDesc &B = d.blocks[k];
-        LtsBlock &L = d.lts[k];
-        const float local = ltsTotalLocal(L, C);
+        local = ltsTotalLocal(L, C);
         // per side: whether the neighbour's layer is received now (with the
         // neighbour's total local time, published at the end of the last
         // iteration; its own check runs at the same time), the border time
@@ -117,65 +123,78 @@ __global__ void ltsCheckKernel(const DomainDev d) {
             sFactor[s] = a == 2 ? local / bt : 0.f;  // interpolateValue: old + (new - old) * (local / remote)
         }
         __syncthreads();
-        // one pass over the perimeter: boundary conditions and corners
-        // (applyBoundaryConditions, src/blocks/SWE_Block.hh:757-911), the
-        // received layer into the receive ring (exchangeGhosts,
-        // src/blocks/SWE_DimensionalSplittingMPIOverdecomp.cpp:273-304), the
-        // ring into the ghost ring of the current buffer
-        const int cur = G->cur;
+    }
+    if (running || stale) {
+        // one pass over the perimeter: the carried ring, then boundary
+        // conditions and corners (applyBoundaryConditions,
+        // src/blocks/SWE_Block.hh:757-911), the received layer into the
+        // receive ring (exchangeGhosts,
+        // src/blocks/SWE_DimensionalSplittingMPIOverdecomp.cpp:273-304) and the
+        // ring into the ghost ring (checkAllGhostlayers)
         float *F[3] = {pick(d.h, cur) + B.base, pick(d.hu, cur) + B.base, pick(d.hv, cur) + B.base};
+        const float *Fo[3] = {pick(d.h, cur ^ 1) + B.base, pick(d.hu, cur ^ 1) + B.base, pick(d.hv, cur ^ 1) + B.base};
         const size_t P = size_t(B.pitch);
         for (int i = threadIdx.x; i < 2 * B.ny + 2 * B.nx + 4; i += blockDim.x) {
-            int side, pos;
+            int side, pos, gx, gy, sx, sy;
             perimeterIndex(B, i, side, pos);
-            if (side == 4) {  // corners from the diagonal interior cell
-                const int gx = (pos & 1) ? B.nx + 1 : 0, gy = (pos & 2) ? B.ny + 1 : 0;
-                const int sx = (pos & 1) ? B.nx : 1, sy = (pos & 2) ? B.ny : 1;
-                for (int f = 0; f < 3; f++) F[f][size_t(gx) * P + gy] = F[f][size_t(sx) * P + sy];
-                continue;
+            if (side == 4) {  // corners: from the diagonal interior cell
+                gx = (pos & 1) ? B.nx + 1 : 0, gy = (pos & 2) ? B.ny + 1 : 0;
+                sx = (pos & 1) ? B.nx : 1, sy = (pos & 2) ? B.ny : 1;
+            } else {
+                ghostCell(B, side, pos, gx, gy, sx, sy);
             }
-            int gx, gy, sx, sy;
-            ghostCell(B, side, pos, gx, gy, sx, sy);
-            const int type = B.bnd[side];
-            if (type == WALL || type == OUTFLOW) {
-                const int negate = (type == WALL) ? (side < 2 ? 1 : 2) : -1;  // hu or hv of a wall, nothing for outflow
-                for (int f = 0; f < 3; f++) {
-                    const float v = F[f][size_t(sx) * P + sy];
-                    F[f][size_t(gx) * P + gy] = (negate == f) ? -v : v;
+            const size_t og = size_t(gx) * P + gy;
+            float g[3];  // the ghost's value now
+            for (int f = 0; f < 3; f++) g[f] = stale ? Fo[f][og] : F[f][og];
+            bool changed = stale;
+            if (running) {
+                const int type = side == 4 ? WALL : B.bnd[side];
+                if (side == 4 || type == WALL || type == OUTFLOW) {
+                    // corners copy the cell; walls negate the normal momentum
+                    const int negate = (side < 4 && type == WALL) ? (side < 2 ? 1 : 2) : -1;
+                    for (int f = 0; f < 3; f++) {
+                        const float v = F[f][size_t(sx) * P + sy];
+                        g[f] = (negate == f) ? -v : v;
+                    }
+                    changed = true;
+                } else {
+                    const long long r = ringOffset(B, side, pos);
+                    float v[3];
+                    if (sRecv[side]) {
+                        const int n = B.nbr[side];
+                        const BlockDesc &N = d.blocks[n];
+                        const int ncur = d.groups[n].cur;
+                        int nx = sx, ny = sy;  // the neighbour's copy layer
+                        switch (side) {
+                        case 0: nx = N.nx; break;
+                        case 1: nx = 1; break;
+                        case 2: ny = N.ny; break;
+                        default: ny = 1; break;
+                        }
+                        const size_t o = size_t(N.base) + size_t(nx) * size_t(N.pitch) + size_t(ny);
+                        v[0] = pick(d.h, ncur)[o];
+                        v[1] = pick(d.hu, ncur)[o];
+                        v[2] = pick(d.hv, ncur)[o];
+                        for (int f = 0; f < 3; f++) d.ring[f][r] = v[f];
+                    }
+                    const int a = sAction[side];
+                    if (a) {
+                        if (!sRecv[side])
+                            for (int f = 0; f < 3; f++) v[f] = d.ring[f][r];
+                        const float factor = sFactor[side];
+                        for (int f = 0; f < 3; f++) g[f] = (a == 1) ? v[f] : g[f] + (v[f] - g[f]) * factor;
+                        changed = true;
+                    }
                 }
-                continue;
             }
-            const long long r = ringOffset(B, side, pos);
-            float v[3];
-            if (sRecv[side]) {
-                const int n = B.nbr[side];
-                const BlockDesc &N = d.blocks[n];
-                const int ncur = d.groups[n].cur;
-                int nx = sx, ny = sy;  // the neighbour's copy layer
-                switch (side) {
-                case 0: nx = N.nx; break;
-                case 1: nx = 1; break;
-                case 2: ny = N.ny; break;
-                default: ny = 1; break;
-                }
-                const size_t o = size_t(N.base) + size_t(nx) * size_t(N.pitch) + size_t(ny);
-                v[0] = pick(d.h, ncur)[o];
-                v[1] = pick(d.hu, ncur)[o];
-                v[2] = pick(d.hv, ncur)[o];
-                for (int f = 0; f < 3; f++) d.ring[f][r] = v[f];
-            }
-            const int a = sAction[side];
-            if (!a) continue;
-            if (!sRecv[side])
-                for (int f = 0; f < 3; f++) v[f] = d.ring[f][r];
-            const float factor = sFactor[side];
-            for (int f = 0; f < 3; f++) {
-                float &g = F[f][size_t(gx) * P + gy];
-                g = (a == 1) ? v[f] : g + (v[f] - g) * factor;
-            }
+            if (changed)
+                for (int f = 0; f < 3; f++) F[f][og] = g[f];
         }
         __syncthreads();
-        if (threadIdx.x == 0) {
+    }
+    if (threadIdx.x == 0) {
+        G->ringStale = 0;
+        if (running) {
             for (int s = 0; s < 4; s++) {
                 const int type = B.bnd[s];
                 if (type != CONNECT && type != CONNECT_WITHIN_RANK) continue;
@@ -190,9 +209,9 @@ __global__ void ltsCheckKernel(const DomainDev d) {
             }
             if (ltsInSync(L) && L.stepSizeCounter < L.stepSize) L.stepSizeCounter++;
             G->enabled = ltsInSync(L) ? 1 : 0;
+        } else {
+            G->enabled = 0;
         }
-    } else if (threadIdx.x == 0) {
-        G->enabled = 0;
     }
     // the last CTA lists the enabled blocks (update pass) and those at the
     // start of their interval (speed pass); the others take Tsync / stepSize,

@@ -251,6 +251,7 @@ __device__ __forceinline__ void segmentDone(const DomainDev &d, GroupState *G, f
             G->steps = G->steps + 1;
             G->cur = cur ^ 1;
             G->ghostsAhead = d.lts ? 0 : 1;  // local time stepping rebuilds the ring itself
+            G->ringStale = d.lts ? 1 : 0;    // ... from the ring the other buffer holds
             // speed bounds now describe the output buffer
             G->boundsValid[cur] = 0;
             G->boundsValid[cur ^ 1] = d.tileW ? 1 : 0;
@@ -352,9 +353,7 @@ static __device__ __noinline__ void pushGhosts(const DomainDev &d, const BlockDe
     for (int side = 0; side < 4; side++) {
         const bool on = side == 0 ? x == 1 : side == 1 ? x == B.nx : side == 2 ? y == 1 : y == B.ny;
         if (!on) continue;
-        // local time stepping rebuilds the ghost ring every iteration from the
-        // ring kept in the new buffer (the reference's single array keeps it)
-        const int type = d.lts ? PASSIVE : B.bnd[side];
+        const int type = B.bnd[side];
         const int gx = side == 0 ? 0 : side == 1 ? B.nx + 1 : x;
         const int gy = side == 2 ? 0 : side == 3 ? B.ny + 1 : y;
         const size_t g = size_t(B.base) + size_t(gx) * P + size_t(gy);
@@ -377,31 +376,15 @@ static __device__ __noinline__ void pushGhosts(const DomainDev &d, const BlockDe
         }
     }
     // corners come from the diagonal interior cell whatever the boundary type
-    // (local time stepping: kept, they are set at the start of each iteration)
     if (edgeX && edgeY) {
         for (int cxi = 0; cxi < 2; cxi++)
             for (int cyi = 0; cyi < 2; cyi++) {
                 const int sx = cxi ? B.nx : 1, sy = cyi ? B.ny : 1;
                 if (sx != x || sy != y) continue;
                 const size_t g = size_t(B.base) + size_t(cxi ? B.nx + 1 : 0) * P + size_t(cyi ? B.ny + 1 : 0);
-                if (d.lts) {
-                    const float *HI = pick(d.h, outBuf ^ 1), *HUI = pick(d.hu, outBuf ^ 1), *HVI = pick(d.hv, outBuf ^ 1);
-                    HO[g] = HI[g]; HUO[g] = HUI[g]; HVO[g] = HVI[g];
-                } else {
-                    HO[g] = h; HUO[g] = hu; HVO[g] = hv;
-                }
+                HO[g] = h; HUO[g] = hu; HVO[g] = hv;
             }
     }
-}
-
-/// writes Q^{n+1} of cell (x, y); rim cells also refresh the ghost layer
-__device__ __forceinline__ void storeCell(const DomainDev &d, const BlockDesc &B, int outBuf, size_t P, int x, int y,
-                                          float h, float hu, float hv) {
-    const size_t o = size_t(B.base) + size_t(x) * P + size_t(y);
-    pick(d.h, outBuf)[o] = h;
-    pick(d.hu, outBuf)[o] = hu;
-    pick(d.hv, outBuf)[o] = hv;
-    if (x == 1 || x == B.nx || y == 1 || y == B.ny) pushGhosts(d, B, outBuf, P, x, y, h, hu, hv);
 }
 
 template <int S, int SEM, bool UPDATE>
@@ -486,12 +469,12 @@ __global__ void __launch_bounds__(kMaxTileRows, 4) sweepKernel(const DomainDev d
         // from the input buffer.  The block's first and last columns go
         // through pushGhosts (corners).  Inline, because the CTA's barrier makes
         // every warp wait for the rim row's warp each column.
-        int rimMode = 0;  // 0: pushGhosts, 1: copy, 2: copy with -hv, 3: keep
+        int rimMode = 0;  // 0: pushGhosts, 1: copy, 2: copy with -hv, 3: keep (local time stepping pushes none)
         long long rimGhost = 0;
         int rimPitch = 0;
-        if (UPDATE && rimRow && B.ny > 1) {
+        if (UPDATE && rimRow && B.ny > 1 && !d.lts) {
             const int side = (y == 1) ? 2 : 3;
-            const int type = d.lts ? PASSIVE : B.bnd[side];
+            const int type = B.bnd[side];
             rimGhost = (side == 2) ? 0 : B.ny + 1;
             rimPitch = B.pitch;
             if (type == OUTFLOW || type == WALL) {
@@ -601,7 +584,9 @@ __global__ void __launch_bounds__(kMaxTileRows, 4) sweepKernel(const DomainDev d
                             HO[o] = hn;
                             HUO[o] = hun;
                             HVO[o] = hvn;
-                            if (x - 1 == 1 || x - 1 == B.nx || rimRow) {
+                            // no ghost pushes under local time stepping: the
+                            // next check carries the ring over and rebuilds it
+                            if (!d.lts && (x - 1 == 1 || x - 1 == B.nx || rimRow)) {
                                 if (rimMode != 0 && x - 1 != 1 && x - 1 != B.nx) {
                                     const long long g = rimGhost + (long long)(x - 1) * rimPitch;
                                     if (rimMode == 3) {
