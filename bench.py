@@ -213,11 +213,12 @@ def accuracy_measure(swe, device, steps=100):
            "against": "FP64 oracle (CPU restatement of the reference's block code in double)", "steps": steps}
     for name in ("fast", "exact"):
         d = states[name] - h64
-        out[name] = {"rel_l1_h": float(np.abs(d).sum() / np.abs(h64).sum()), "max_abs_dh": float(np.abs(d).max()),
+        out[name] = {"rel_l1_h": float(np.abs(d).sum() / np.abs(h64).sum()),
+                     "rel_linf_h": float(np.abs(d).max() / np.abs(h64).max()), "max_abs_dh": float(np.abs(d).max()),
                      "mass_drift_rel": float(abs(states[name].sum() - m0) / m0)}
     out["exact"]["note"] = "bit-identical to the FP32 oracle (the reference's float arithmetic)"
     out["fp64_mass_drift_rel"] = float(abs(h64.sum() - m0) / m0)
-    out["clamp_mass"] = 0.0
+    out["clamp_mass"] = float(R.clamp_mass)  # depth the FP64 run's dry clamp added
     return out
 
 
@@ -562,6 +563,9 @@ def ensemble_measure(swe, device, steps=100, count=256):
     # warm-up's 16 plus the timed ones)
     oracle.build()
     errs = {"fast": [], "exact": []}
+    linf = {"fast": [], "exact": []}
+    mass = {"fast": [], "exact": [], "fp64": []}
+    clamp = 0.0
     off = 0
     for i in range(8):
         nx, ny, dx, dy, bnd = inst[i]
@@ -571,15 +575,24 @@ def ensemble_measure(swe, device, steps=100, count=256):
         R.bathymetry_ghosts()
         R.step(finals["fast"][1])
         h64 = R.get_state(np.float64)[0]
+        clamp += float(R.clamp_mass)
         a = np.zeros((nx + 2, ny + 2), bool)
         a[1:-1, 1:-1] = True
         a = a.ravel()
+        m0 = float(np.sum(states[i][0][a].astype(np.float64)))
+        mass["fp64"].append(abs(float(h64[a].sum()) - m0) / m0)
         for name in ("fast", "exact"):
             g = finals[name][0][off:off + sz].astype(np.float64)
             errs[name].append(float(np.abs(g[a] - h64[a]).sum() / np.abs(h64[a]).sum()))
+            linf[name].append(float(np.abs(g[a] - h64[a]).max() / np.abs(h64[a]).max()))
+            mass[name].append(abs(float(g[a].sum()) - m0) / m0)
         off += sz
     out["fp64_first8"] = {"steps": finals["fast"][1], "rel_l1_h_fast_max": max(errs["fast"]),
-                          "rel_l1_h_exact_max": max(errs["exact"])}
+                          "rel_l1_h_exact_max": max(errs["exact"]), "rel_linf_h_fast_max": max(linf["fast"]),
+                          "rel_linf_h_exact_max": max(linf["exact"]), "mass_change_rel_fast_max": max(mass["fast"]),
+                          "mass_change_rel_exact_max": max(mass["exact"]), "mass_change_rel_fp64_max": max(mass["fp64"]),
+                          "clamp_mass_fp64": clamp,
+                          "note": "mass change: flow through open sides plus depth the dry clamp added"}
     return out
 
 
