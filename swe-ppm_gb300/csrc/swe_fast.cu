@@ -483,7 +483,20 @@ __global__ void __launch_bounds__(kMaxTileRows / (2 * NP), MINB) fastStepKernel(
 
     const int t = threadIdx.x, lane = t & 31, nth = blockDim.x, nw = nth >> 5, TY = R * nth;
     // strips start as a state at rest (rows a partial tile never loads stay finite)
-    for (int i = t; i < kRing * kSlotFloats; i += nth) ring[i] = ((i % kSlotFloats) < kSlice) ? 1.f : 0.f;
+#pragma unroll
+    for (int s = 0; s < kRing; s++)
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+            for (int i = t; i < kSlice; i += nth) ring[s * kSlotFloats + q * kSlice + i] = q == 0 ? 1.f : 0.f;
+    // the partition and the block descriptors are written only when the
+    // domain is built: bring the first segment's into L1 before the wait
+    if (t == 0) {
+        const int s0 = f.ctaSeg[blockIdx.x];
+        if (s0 < f.ctaSeg[blockIdx.x + 1]) {
+            prefetchL1(&f.units[s0]);
+            prefetchL1(&f.d.blocks[f.units[s0].block]);
+        }
+    }
     if (t == 0) {
         for (int s = 0; s < kRing; s++) {
             mbarInit(smemAddr(&mbar[s]), 1u);
