@@ -36,6 +36,12 @@ namespace solver {
 
 template <typename T> class AugRie {
 public:
+    // Defaults: the reference default-constructs its solver
+    // (src/blocks/SWE_DimensionalSplittingMpi.hh:84-87) from the swe_solvers
+    // module, absent from the reference checkout, so they are unpinned.  The
+    // single Newton iteration with tolerance 1e-6 is George 2008's solver as
+    // GeoClaw calls it (riemann_aug_JCP); dryTol 0.01 and zeroTol 1e-7 are the
+    // module's default-construction values.
     explicit AugRie(T dryTol = T(0.01), T gravity = T(9.81), T newtonTol = T(1e-6),
                     int maxNewtonIterations = 1, T zeroTol = T(1e-7))
         : dryTol_(dryTol), g_(gravity), newtonTol_(newtonTol), maxNewton_(maxNewtonIterations),

@@ -24,8 +24,8 @@ namespace swegb {
 constexpr float kG = 9.81f;
 constexpr float kHalfG = 0.5f * 9.81f;  // exact in float
 constexpr float kSqrtG = 0x1.90e864p+1f;  // sqrtf(9.81f), correctly rounded
-constexpr float kDryTol = 0.01f;        // solver dry tolerance
-constexpr float kZeroTol = 1e-7f;       // |s| below this: wave split evenly
+constexpr float kDryTol = 0.01f;        // solver dry tolerance (swe_solvers' default; see AugRieParams)
+constexpr float kZeroTol = 1e-7f;       // |s| below this: wave split evenly (the same)
 constexpr int kColPad = 31;             // y = 0 sits at offset 31 of a column
 constexpr int kMaxTileRows = 256;       // threads per CTA (one row each)
 constexpr int kMaxTileCols = 128;       // columns per x-chunk
@@ -326,6 +326,13 @@ template <int S> __device__ __forceinline__ float edgeSpeedFH(Cell L, Cell R) {
 // Augmented Riemann solver (George 2008): per-edge, same operation order as
 // the CPU restatement it is tested against.
 // ---------------------------------------------------------------------------
+// The reference default-constructs its solvers (src/blocks/SWE_DimensionalSplittingMpi.hh:84-87)
+// from the swe_solvers module, which is not part of the reference checkout,
+// so these values cannot be checked against it.  They are those of the
+// published augmented solver: George 2008's method as GeoClaw calls it
+// (riemann_aug_JCP with a single Newton iteration for the middle state,
+// tolerance 1e-6), with zeroTol (1e-7) and dryTol (0.01) above as the
+// default-construction values of swe_solvers' solver classes.
 struct AugRieParams {
     static constexpr float newtonTol = 1e-6f;
     static constexpr int maxNewton = 1;
