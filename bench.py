@@ -596,6 +596,48 @@ def ensemble_measure(swe, device, steps=100, count=256):
     return out
 
 
+def drivers_measure():
+    """The driver executable (swe-ppm_gb300/_build/swe_gb300, the reference
+    drivers' flags) on two of the reference's run lines, timed by the
+    driver's own wall clock around its checkpoint loop, which includes the
+    asynchronous snapshots and the NetCDF writes (-w 1, one file per block,
+    as the reference's WALL_TIME covers its writer): the 256^2 radial dam
+    break with the hybrid solver to 10 s in 5 checkpoints, and the 2048^2
+    tsunami as 4 x 4 blocks to 80 s in 20 checkpoints in both arithmetics."""
+    import shutil
+    import tempfile
+    exe = os.path.join(ROOT, "swe-ppm_gb300", "_build", "swe_gb300")
+    runs = {
+        "radial_dam_break_256_hybrid_10s": ["-t", "10", "-n", "5", "-x", "256", "-y", "256", "--scenario",
+                                            "radial_dam_break", "--solver", "hybrid"],
+        "tsunami_2048_80s_fast": ["-t", "80", "-n", "20", "-x", "2048", "-y", "2048", "--blocks", "16", "--scenario",
+                                  "tsunami", "--solver", "hlle", "--arithmetic", "fast"],
+        "tsunami_2048_80s_exact": ["-t", "80", "-n", "20", "-x", "2048", "-y", "2048", "--blocks", "16", "--scenario",
+                                   "tsunami", "--solver", "hlle"],
+    }
+    out = {"note": "wall clock of the driver's checkpoint loop, NetCDF output included"}
+    tmp = tempfile.mkdtemp(prefix="swe_drivers_")
+    try:
+        for name, args in runs.items():
+            r = subprocess.run([exe] + args + ["-w", "1", "-o", os.path.join(tmp, name)], capture_output=True,
+                               text=True, timeout=900)
+            vals = {}
+            for line in r.stdout.splitlines():
+                if ":" in line:
+                    k, v = line.split(":", 1)
+                    vals[k.strip()] = v.strip()
+            if r.returncode != 0 or "Wall Time" not in vals:
+                out[name] = {"error": (r.stderr or r.stdout)[-300:]}
+                continue
+            files = [f for f in os.listdir(tmp) if f.startswith(name) and f.endswith(".nc")]
+            out[name] = {"wall_s": float(vals["Wall Time"].rstrip("s")), "steps": int(vals["Steps"]),
+                         "cell_updates_per_s": float(vals["Cell updates"].split("/")[0]),
+                         "netcdf_bytes": int(sum(os.path.getsize(os.path.join(tmp, f)) for f in files))}
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+    return out
+
+
 def split_measure(swe, device, steps=20):
     """The split step (SWE_DimensionalSplitting: x-sweep over the ghost rows,
     dt from the x-sweep's speeds, y-sweep with dt/dx) on the same tsunami
@@ -983,6 +1025,7 @@ def run_gb300(args, world, rank, local):
     ens = ensemble_measure(swe, local)
     sur = surrogate_measure(swe, local) if rank == 0 else None
     split = split_measure(swe, local) if rank == 0 else None
+    drivers = drivers_measure() if rank == 0 else None
     base = cpu_reference_baseline(args) if rank == 0 else None
     clocks = clk.summary()
     issue = None
@@ -1018,7 +1061,7 @@ def run_gb300(args, world, rank, local):
                     "d2h_bytes_per_step": d2h, "calls": "upload_async, step, download_async; sync at the end",
                     "synchronous_value": world * cells / e2e_sync_s},
             "clocks": clocks, "gpu_launches": launches, "device_status": status,
-            "lts": lts, "ensemble": ens, "surrogate": sur, "split": split,
+            "lts": lts, "ensemble": ens, "surrogate": sur, "split": split, "drivers": drivers,
         }
         print(json.dumps(line), flush=True)
     dist_barrier(world)

@@ -4,8 +4,9 @@
 // swe_mpi_overdecomp.cpp): -t simulated seconds, -n checkpoints, -x/-y cells,
 // -o output base name, -w 1 to write NetCDF files (one per block, like one per
 // rank), plus --blocks N (overdecomposition into a near-square block grid),
-// --solver hlle|fwave|augrie|hybrid, --semantics unsplit|split, --scenario and
-// --seed.  The time loop `while (t < checkpoint) step` of
+// --solver hlle|fwave|augrie|hybrid, --semantics unsplit|split, --scenario,
+// --seed and --arithmetic exact|fast (the fast-arithmetic step of the f-wave
+// and HLLE solvers).  The time loop `while (t < checkpoint) step` of
 // src/examples/swe_mpi.cpp:300-327 runs on the device (swe_gpu_advance, or
 // swe_gpu_lts_advance with -l > 0: local time stepping with intervals of that
 // length, src/examples/swe_mpi_overdecomp.cpp:308-343); at
@@ -69,6 +70,7 @@ struct Slot {
 int main(int argc, char **argv) {
     float duration = 0.f;
     int checkpoints = 1, nx = 0, ny = 0, nblocks = 1, write = 0, semantics = SWE_SEMANTICS_UNSPLIT;
+    int arithmetic = SWE_ARITH_EXACT;
     float ltsInterval = 0.f;  // -l: local time stepping with intervals of this length
     std::string out = "swe", scenario = "radial_bathymetry_dam_break", solver = "hlle";
     double seed = 20261203;
@@ -84,9 +86,10 @@ int main(int argc, char **argv) {
                             {"semantics", required_argument, 0, 'm'},
                             {"scenario", required_argument, 0, 'c'},
                             {"seed", required_argument, 0, 'e'},
+                            {"arithmetic", required_argument, 0, 'a'},
                             {0, 0, 0, 0}};
     int c;
-    while ((c = getopt_long(argc, argv, "t:n:x:y:o:w:l:b:s:m:c:e:", opts, nullptr)) != -1) {
+    while ((c = getopt_long(argc, argv, "t:n:x:y:o:w:l:b:s:m:c:e:a:", opts, nullptr)) != -1) {
         switch (c) {
         case 't': duration = float(atof(optarg)); break;
         case 'n': checkpoints = atoi(optarg); break;
@@ -100,9 +103,11 @@ int main(int argc, char **argv) {
         case 'm': semantics = std::string(optarg) == "split" ? SWE_SEMANTICS_SPLIT : SWE_SEMANTICS_UNSPLIT; break;
         case 'c': scenario = optarg; break;
         case 'e': seed = atof(optarg); break;
+        case 'a': arithmetic = std::string(optarg) == "fast" ? SWE_ARITH_FAST : SWE_ARITH_EXACT; break;
         default:
             fprintf(stderr, "usage: %s -t seconds -n checkpoints -x nx -y ny [-o base] [-w 1] [--blocks N] "
-                            "[--solver hlle|fwave|augrie|hybrid] [--semantics unsplit|split] [--scenario name]\n",
+                            "[--solver hlle|fwave|augrie|hybrid] [--semantics unsplit|split] [--scenario name] "
+                            "[--arithmetic exact|fast]\n",
                     argv[0]);
             return 1;
         }
@@ -149,6 +154,7 @@ int main(int argc, char **argv) {
     d.semantics = semantics;
     d.lts_max_timestep = ltsInterval;
     d.duration = duration;
+    d.arithmetic = arithmetic;
     swe_gpu_domain *dom = nullptr;
     if (swe_gpu_domain_create(&d, &dom)) die("swe_gpu_domain_create");
 
