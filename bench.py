@@ -7,18 +7,20 @@ stepping.  One bench step = one time step (ghost layer + fluxes/dt + update)
 of the whole domain.  Metric: cell-updates/s (higher is better).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                  [--arith fast|exact]
 
-gb300 arm: state resident in HBM; L2 (126 MB) is flushed by writing 256 MB
-between timed steps (the 2048^2 state, 67 MB, would otherwise stay in L2);
-each step is timed with CUDA events on the library's stream.  `e2e` runs the
-same steps through the C ABI on host buffers: upload h, hu, hv, b from pinned
-memory, step, download h, hu, hv, timed on the host clock.  `roofline` is the
-fused update kernel's algorithmic bytes (28 B/cell) over its event-timed
-duration; `cpu_baseline` times the oracle (CPU restatement of the reference's
-algorithm) on the host cores for a bounded sample of the same workload.
-reference arm: the oracle on all host cores (the reference's own compiled
-code cannot run on the GPU host: its solver module is absent and its
-sources are not shipped), one bounded sample per step.
+gb300 arm: the fast-arithmetic step (one launch per step; the bit-exact step
+is reported beside it); state resident in HBM; L2 (126 MB) is flushed by
+writing 256 MB between timed steps (the 2048^2 state, 67 MB, would otherwise
+stay in L2); each step is timed with CUDA events on the library's stream.
+`e2e` runs the same steps through the C ABI on host buffers: upload h, hu,
+hv, b from pinned memory, step, download h, hu, hv, timed on the host clock.
+`roofline` is the step kernel's algorithmic bytes (28 B/cell) over its
+event-timed duration.  `cpu_baseline` times the reference's own stock CPU
+benchmark driver (swe_benchmark_mpioverdecomp, built on this host from the
+staged reference sources) on all host cores for a bounded span, or, without
+those sources, the oracle (the CPU restatement of the reference's block code).
+reference arm: the same CPU leg, one bounded sample per step.
 Multi-GPU: replicas only (independent copies, no collective in the step);
 value = all ranks' cell updates / max-over-ranks time.
 """
