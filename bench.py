@@ -677,9 +677,12 @@ def split_measure(swe, device, steps=20):
 def surrogate_measure(swe, device, steps=10, err_steps=120):
     """MLP surrogate of the augmented Riemann solver at 4096^2: the shoreline
     ramp (bathymetry -4000 m to +50 m across 50 km, seeded Gaussian bump) as
-    4x4 blocks of 1024^2, unsplit.  Training data: every 64th wet edge logged
-    at steps 10, 20, 30, 40 of an augmented-solver run; 8 epochs of Adam on the
-    device.  Timed (CUDA events, `steps` steps after warm-up): the augmented
+    4x4 blocks of 1024^2, unsplit.  Training data: about 1e7 wet-edge states
+    with their augmented-solver net updates, logged from augmented-solver runs
+    of the benchmark's configurations 1 and 2 (the 256^2 radial dam break, every
+    edge at 20 instants; the 2048^2 tsunami as 4x4 blocks, every 8th edge at 6
+    instants) and of this workload (every 64th edge at 4 instants); 8 epochs
+    of Adam on the device.  Timed (CUDA events, `steps` steps after warm-up): the augmented
     solver's default step (each edge solved once into the edge buffers), its
     two-pass step (speed pass + update pass, each edge solved twice), and the
     surrogate step.  Accuracy: each solver runs `err_steps` steps from the
@@ -699,14 +702,27 @@ def surrogate_measure(swe, device, steps=10, err_steps=120):
         D.exchange_bathymetry()
         return D
 
-    A = make(swe.AUGRIE)
     E, T = [], []
-    for _ in range(4):
-        A.step(10)
-        e, t = A.log_edges(stride=64, capacity=1 << 21)
-        E.append(e)
-        T.append(t)
-    A.close()
+
+    def log_run(D, logs, every, stride):
+        for _ in range(logs):
+            D.step(every)
+            e, t = D.log_edges(stride=stride, capacity=1 << 21)
+            E.append(e)
+            T.append(t)
+        D.close()
+
+    for scen, nn, nblk, params, logs, every, stride in (
+            (swe.SCENARIO_RADIAL_DAM_BREAK, 256, 1, None, 20, 2, 1),
+            (swe.SCENARIO_TSUNAMI, 2048, 16, [2048, SEED, 100000.0], 6, 10, 8)):
+        g2, *s2 = swe.init_domain(scen, nn, nn, nblk, params)
+        D2 = swe.Domain(g2["nx_cols"], g2["ny_rows"], g2["dx"], g2["dy"], boundary=g2["boundary"],
+                        solver=swe.AUGRIE, device=device)
+        D2.set_stream(stream.cuda_stream)
+        D2.upload(*s2)
+        D2.exchange_bathymetry()
+        log_run(D2, logs, every, stride)
+    log_run(make(swe.AUGRIE), 4, 10, 64)
     E, T = np.concatenate(E, axis=1), np.concatenate(T, axis=1)
     m = swe.Surrogate(seed=SEED)
     epochs = 8
