@@ -84,18 +84,26 @@ __global__ void ltsCheckKernel(const DomainDev d) {
     __shared__ float sFactor[4];
     __shared__ int sLast;
     __shared__ int sScan[4][kLtsCheckThreads];
+    __shared__ LtsBlock L;   // the block's state, staged: its reads and writes stay on chip
+    __shared__ int sCur, sStale;
+    static_assert(sizeof(LtsBlock) % 4 == 0 && sizeof(LtsBlock) / 4 <= kLtsCheckThreads, "staging");
     pdlWaitAndRelease();
     const int k = blockIdx.x;
     GroupState *G = d.groups + k;
     const LtsControl C = *d.ltsCtl;
     const bool running = ltsRunning(C);
     const BlockDesc &B = d.blocks[k];
-    LtsBlock &L = d.lts[k];
-    const int cur = G->cur;
+    constexpr int kLInts = int(sizeof(LtsBlock) / 4);
+    if (threadIdx.x < kLInts)
+        reinterpret_cast<int *>(&L)[threadIdx.x] = reinterpret_cast<const int *>(d.lts + k)[threadIdx.x];
+    if (threadIdx.x == kLInts) sCur = G->cur;
     // the update pass writes no ghosts: after it the current buffer's ring
     // (and corners) are still in the other buffer; the reference's single
     // array keeps them, so they are carried over first
-    const bool stale = G->ringStale != 0;
+    if (threadIdx.x == kLInts + 1) sStale = G->ringStale;
+    __syncthreads();
+    const int cur = sCur;
+    const bool stale = sStale != 0;
     float local = 0.f;
     if (running) {
         local = ltsTotalLocal(L, C);
@@ -193,7 +201,7 @@ __global__ void ltsCheckKernel(const DomainDev d) {
         __syncthreads();
     }
     if (threadIdx.x == 0) {
-        G->ringStale = 0;
+        if (stale) G->ringStale = 0;
         if (running) {
             for (int s = 0; s < 4; s++) {
                 const int type = B.bnd[s];
@@ -212,6 +220,12 @@ __global__ void ltsCheckKernel(const DomainDev d) {
         } else {
             G->enabled = 0;
         }
+    }
+    // the block's state back to global memory
+    __syncthreads();
+    if (running && threadIdx.x < kLInts) {
+        reinterpret_cast<int *>(d.lts + k)[threadIdx.x] = reinterpret_cast<const int *>(&L)[threadIdx.x];
+        __threadfence();
     }
     // the last CTA lists the enabled blocks (update pass) and those at the
     // start of their interval (speed pass); the others take Tsync / stepSize,
@@ -234,10 +248,18 @@ __global__ void ltsCheckKernel(const DomainDev d) {
             spd = upd && __ldcg(&d.lts[j].stepSizeCounter) <= 0;
         };
         int v[4] = {0, 0, 0, 0};  // enabled blocks, their pairs, interval starts, their pairs
+        constexpr int kCache = 4;  // the first entries' values, kept for the second pass
+        int cPairs[kCache];
+        bool cUpd[kCache], cSpd[kCache];
         for (int j = j0; j < j1; j++) {
             int pairs;
             bool upd, spd;
             entry(j, pairs, upd, spd);
+            if (j - j0 < kCache) {
+                cPairs[j - j0] = pairs;
+                cUpd[j - j0] = upd;
+                cSpd[j - j0] = spd;
+            }
             if (upd) {
                 v[0]++;
                 v[1] += pairs;
@@ -265,7 +287,13 @@ __global__ void ltsCheckKernel(const DomainDev d) {
         for (int j = j0; j < j1; j++) {
             int pairs;
             bool upd, spd;
-            entry(j, pairs, upd, spd);
+            if (j - j0 < kCache) {
+                pairs = cPairs[j - j0];
+                upd = cUpd[j - j0];
+                spd = cSpd[j - j0];
+            } else {
+                entry(j, pairs, upd, spd);
+            }
             if (upd) {
                 pU[o[0]] = o[1];
                 lU[o[0]++] = j;
