@@ -64,17 +64,14 @@ __device__ __forceinline__ long long ringOffset(const BlockDesc &B, int side, in
     }
 }
 
-/// decodes thread index i of a block's perimeter into (side, position);
-/// side 4 = corner 0..3
-__device__ __forceinline__ bool perimeterIndex(const BlockDesc &B, int i, int &side, int &pos) {
+/// decodes thread index i of a block's perimeter (corners excluded) into
+/// (side, position)
+__device__ __forceinline__ void perimeterIndex(const BlockDesc &B, int i, int &side, int &pos) {
     const int nx = B.nx, ny = B.ny;
     if (i < ny) { side = 0; pos = i + 1; }
     else if (i < 2 * ny) { side = 1; pos = i - ny + 1; }
     else if (i < 2 * ny + nx) { side = 2; pos = i - 2 * ny + 1; }
-    else if (i < 2 * ny + 2 * nx) { side = 3; pos = i - 2 * ny - nx + 1; }
-    else if (i < 2 * ny + 2 * nx + 4) { side = 4; pos = i - 2 * ny - 2 * nx; }
-    else return false;
-    return true;
+    else { side = 3; pos = i - 2 * ny - nx + 1; }
 }
 
 /// exchangeGhosts + checkAllGhostlayers (src/blocks/SWE_Block.hh:375-436):
@@ -82,25 +79,39 @@ __device__ __forceinline__ bool perimeterIndex(const BlockDesc &B, int i, int &s
 __global__ void ltsCheckKernel(const DomainDev d) {
     __shared__ int sAction[4], sRecv[4];  // per side: 0 none, 1 copy, 2 interpolate; layer received now
     __shared__ float sFactor[4];
+    __shared__ float sNbrLocal[4];  // per side within the rank: the neighbour's total local time
+    __shared__ int sNbrCur[4];      // and its current buffer
     __shared__ int sLast;
-    __shared__ int sScan[4][kLtsCheckThreads];
+    __shared__ int sScan[4][kLtsCheckThreads / 32];
     __shared__ LtsBlock L;   // the block's state, staged: its reads and writes stay on chip
     __shared__ int sCur, sStale;
-    static_assert(sizeof(LtsBlock) % 4 == 0 && sizeof(LtsBlock) / 4 <= kLtsCheckThreads, "staging");
+    static_assert(sizeof(LtsBlock) % 4 == 0 && sizeof(LtsBlock) / 4 + 2 <= 32, "staging by warp 0");
+    static_assert(kLtsCheckThreads % 32 == 0 && kLtsCheckThreads <= 1024, "warp scan");
     pdlWaitAndRelease();
-    const int k = blockIdx.x;
+    const int k = blockIdx.x, t = threadIdx.x;
     GroupState *G = d.groups + k;
     const LtsControl C = *d.ltsCtl;
     const bool running = ltsRunning(C);
     const BlockDesc &B = d.blocks[k];
     constexpr int kLInts = int(sizeof(LtsBlock) / 4);
-    if (threadIdx.x < kLInts)
-        reinterpret_cast<int *>(&L)[threadIdx.x] = reinterpret_cast<const int *>(d.lts + k)[threadIdx.x];
-    if (threadIdx.x == kLInts) sCur = G->cur;
-    // the update pass writes no ghosts: after it the current buffer's ring
-    // (and corners) are still in the other buffer; the reference's single
-    // array keeps them, so they are carried over first
-    if (threadIdx.x == kLInts + 1) sStale = G->ringStale;
+    // one round of loads: the block's state (warp 0) and, per side connected
+    // within the rank, the neighbour's local time published at the end of the
+    // last iteration and its current buffer (warp 1; the neighbour's own
+    // check, running at the same time, writes neither)
+    if (t < kLInts) {
+        reinterpret_cast<int *>(&L)[t] = reinterpret_cast<const int *>(d.lts + k)[t];
+    } else if (t == kLInts) {
+        sCur = G->cur;
+    } else if (t == kLInts + 1) {
+        // the update pass writes no ghosts: after it the current buffer's
+        // ring (and corners) are still in the other buffer; the reference's
+        // single array keeps them, so they are carried over first
+        sStale = G->ringStale;
+    } else if (t >= 32 && t < 36 && B.bnd[t - 32] == CONNECT_WITHIN_RANK) {
+        const int n = B.nbr[t - 32];
+        sNbrLocal[t - 32] = __ldcg(&d.ltsLocal[n]);
+        sNbrCur[t - 32] = __ldcg(&d.groups[n].cur);
+    }
     __syncthreads();
     const int cur = sCur;
     const bool stale = sStale != 0;
@@ -108,18 +119,17 @@ __global__ void ltsCheckKernel(const DomainDev d) {
     if (running) {
         local = ltsTotalLocal(L, C);
         // per side: whether the neighbour's layer is received now (with the
-        // neighbour's total local time, published at the end of the last
-        // iteration; its own check runs at the same time), the border time
-        // after that, and what checkAllGhostlayers does with the layer: copy
-        // (same time) or interpolate (neighbour ahead)
-        if (threadIdx.x < 4) {
-            const int s = threadIdx.x;
+        // neighbour's total local time), the border time after that, and
+        // what checkAllGhostlayers does with the layer: copy (same time) or
+        // interpolate (neighbour ahead)
+        if (t < 4) {
+            const int s = t;
             const int type = B.bnd[s];
             int recv = 0, a = 0;
             float bt = L.borderTimestep[s];
             if (type == CONNECT_WITHIN_RANK && ltsReceivable(L, s)) {
                 recv = 1;
-                bt = __ldcg(&d.ltsLocal[B.nbr[s]]);
+                bt = sNbrLocal[s];
                 L.borderTimestep[s] = bt;
             }
             if (type == CONNECT || type == CONNECT_WITHIN_RANK) {
@@ -142,24 +152,30 @@ __global__ void ltsCheckKernel(const DomainDev d) {
         float *F[3] = {pick(d.h, cur) + B.base, pick(d.hu, cur) + B.base, pick(d.hv, cur) + B.base};
         const float *Fo[3] = {pick(d.h, cur ^ 1) + B.base, pick(d.hu, cur ^ 1) + B.base, pick(d.hv, cur ^ 1) + B.base};
         const size_t P = size_t(B.pitch);
-        for (int i = threadIdx.x; i < 2 * B.ny + 2 * B.nx + 4; i += blockDim.x) {
+        // corners copy the diagonal interior cell (or, carried only, the
+        // other buffer's corner); threads 0..3 load them ahead of their side
+        // positions and store them after, so both loads are in flight at once
+        float cv[3];
+        size_t cog = 0;
+        if (t < 4) {
+            const int gx = (t & 1) ? B.nx + 1 : 0, gy = (t & 2) ? B.ny + 1 : 0;
+            const int sx = (t & 1) ? B.nx : 1, sy = (t & 2) ? B.ny : 1;
+            cog = size_t(gx) * P + gy;
+            for (int f = 0; f < 3; f++) cv[f] = running ? F[f][size_t(sx) * P + sy] : Fo[f][cog];
+        }
+        for (int i = t; i < 2 * B.ny + 2 * B.nx; i += blockDim.x) {
             int side, pos, gx, gy, sx, sy;
             perimeterIndex(B, i, side, pos);
-            if (side == 4) {  // corners: from the diagonal interior cell
-                gx = (pos & 1) ? B.nx + 1 : 0, gy = (pos & 2) ? B.ny + 1 : 0;
-                sx = (pos & 1) ? B.nx : 1, sy = (pos & 2) ? B.ny : 1;
-            } else {
-                ghostCell(B, side, pos, gx, gy, sx, sy);
-            }
+            ghostCell(B, side, pos, gx, gy, sx, sy);
             const size_t og = size_t(gx) * P + gy;
             float g[3];  // the ghost's value now
             for (int f = 0; f < 3; f++) g[f] = stale ? Fo[f][og] : F[f][og];
             bool changed = stale;
             if (running) {
-                const int type = side == 4 ? WALL : B.bnd[side];
-                if (side == 4 || type == WALL || type == OUTFLOW) {
-                    // corners copy the cell; walls negate the normal momentum
-                    const int negate = (side < 4 && type == WALL) ? (side < 2 ? 1 : 2) : -1;
+                const int type = B.bnd[side];
+                if (type == WALL || type == OUTFLOW) {
+                    // walls negate the normal momentum
+                    const int negate = type == WALL ? (side < 2 ? 1 : 2) : -1;
                     for (int f = 0; f < 3; f++) {
                         const float v = F[f][size_t(sx) * P + sy];
                         g[f] = (negate == f) ? -v : v;
@@ -169,9 +185,8 @@ __global__ void ltsCheckKernel(const DomainDev d) {
                     const long long r = ringOffset(B, side, pos);
                     float v[3];
                     if (sRecv[side]) {
-                        const int n = B.nbr[side];
-                        const BlockDesc &N = d.blocks[n];
-                        const int ncur = d.groups[n].cur;
+                        const BlockDesc &N = d.blocks[B.nbr[side]];
+                        const int ncur = sNbrCur[side];
                         int nx = sx, ny = sy;  // the neighbour's copy layer
                         switch (side) {
                         case 0: nx = N.nx; break;
@@ -198,9 +213,11 @@ __global__ void ltsCheckKernel(const DomainDev d) {
             if (changed)
                 for (int f = 0; f < 3; f++) F[f][og] = g[f];
         }
+        if (t < 4)
+            for (int f = 0; f < 3; f++) F[f][cog] = cv[f];
         __syncthreads();
     }
-    if (threadIdx.x == 0) {
+    if (t == 0) {
         if (stale) G->ringStale = 0;
         if (running) {
             for (int s = 0; s < 4; s++) {
@@ -223,15 +240,15 @@ __global__ void ltsCheckKernel(const DomainDev d) {
     }
     // the block's state back to global memory
     __syncthreads();
-    if (running && threadIdx.x < kLInts) {
-        reinterpret_cast<int *>(d.lts + k)[threadIdx.x] = reinterpret_cast<const int *>(&L)[threadIdx.x];
+    if (running && t < kLInts) {
+        reinterpret_cast<int *>(d.lts + k)[t] = reinterpret_cast<const int *>(&L)[t];
         __threadfence();
     }
     // the last CTA lists the enabled blocks (update pass) and those at the
     // start of their interval (speed pass); the others take Tsync / stepSize,
     // the step the speed pass would round to (SWE_Block::getRoundTimestep)
     __syncthreads();
-    if (threadIdx.x == 0)
+    if (t == 0)
         sLast = arriveAcqRel(reinterpret_cast<unsigned *>(d.ltsWork + kLwArrCheck), 1u) + 1u == gridDim.x;
     __syncthreads();
     if (sLast) {
@@ -271,17 +288,32 @@ __global__ void ltsCheckKernel(const DomainDev d) {
                 d.groups[j].dt = C.maxTimestepLocal / float(__ldcg(&d.lts[j].stepSize));
             }
         }
-        for (int q = 0; q < 4; q++) sScan[q][i] = v[q];
+        // exclusive scans of the four counts over the CTA: within each warp
+        // by shuffles, then over the warps' totals
+        const int lane = i & 31, warp = i >> 5, nwarps = T >> 5;
+        int c[4];
+        for (int q = 0; q < 4; q++) c[q] = v[q];
+        for (int off = 1; off < 32; off *= 2)
+            for (int q = 0; q < 4; q++) {
+                const int w = __shfl_up_sync(0xffffffffu, c[q], off);
+                if (lane >= off) c[q] += w;
+            }
+        if (lane == 31)
+            for (int q = 0; q < 4; q++) sScan[q][warp] = c[q];
         __syncthreads();
-        for (int off = 1; off < T; off *= 2) {  // inclusive scans (Hillis-Steele)
-            int w[4];
-            for (int q = 0; q < 4; q++) w[q] = i >= off ? sScan[q][i - off] : 0;
-            __syncthreads();
-            for (int q = 0; q < 4; q++) sScan[q][i] += w[q];
-            __syncthreads();
+        if (warp == 0) {
+            for (int q = 0; q < 4; q++) {
+                int w = lane < nwarps ? sScan[q][lane] : 0;
+                for (int off = 1; off < 32; off *= 2) {
+                    const int u = __shfl_up_sync(0xffffffffu, w, off);
+                    if (lane >= off) w += u;
+                }
+                if (lane < nwarps) sScan[q][lane] = w;
+            }
         }
+        __syncthreads();
         int o[4];
-        for (int q = 0; q < 4; q++) o[q] = sScan[q][i] - v[q];
+        for (int q = 0; q < 4; q++) o[q] = c[q] - v[q] + (warp ? sScan[q][warp - 1] : 0);
         int *lU = lwList(W, nb, true), *pU = lwPrefix(W, nb, true);
         int *lS = lwList(W, nb, false), *pS = lwPrefix(W, nb, false);
         for (int j = j0; j < j1; j++) {
