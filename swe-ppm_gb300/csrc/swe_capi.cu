@@ -281,6 +281,10 @@ struct swe_gpu_domain {
     long long ringElems = 0;
     cudaGraphExec_t ltsGraph = nullptr;
     long long ltsGraphKernels = 0;
+    // the control block after each of two replays in flight (pinned) and
+    // the events that mark its copy
+    LtsControl *ltsCtlHost = nullptr;
+    cudaEvent_t ltsCtlReady[2] = {nullptr, nullptr};
     // surrogate step and edge logger: edge tiles and the stored net updates
     std::vector<mlp::EdgeTile> edgeTiles;
     mlp::EdgeTile *dEdgeTiles = nullptr;
@@ -486,6 +490,9 @@ void freeDomain(swe_gpu_domain *D) {
     cudaFree(D->dLtsWork);
     cudaFree(D->dLtsLocal);
     for (int f = 0; f < 3; f++) cudaFree(D->dRing[f]);
+    if (D->ltsCtlHost) cudaFreeHost(D->ltsCtlHost);
+    for (int j = 0; j < 2; j++)
+        if (D->ltsCtlReady[j]) cudaEventDestroy(D->ltsCtlReady[j]);
     if (D->snapEvent) cudaEventDestroy(D->snapEvent);
     for (int i = 0; i < 2; i++) {
         cudaFree(D->h[i]);
@@ -1533,6 +1540,14 @@ int swe_gpu_lts_advance(swe_gpu_domain *dom, float t_end, int max_iterations, in
         cudaGraphDestroy(g);
         if (e != cudaSuccess) return fail(SWE_GPU_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
     }
+    if (!dom->ltsCtlHost) {
+        cudaError_t e = cudaMallocHost(&dom->ltsCtlHost, 2 * sizeof(LtsControl));
+        if (e != cudaSuccess) {
+            dom->ltsCtlHost = nullptr;
+            return fail(SWE_GPU_ERR_NOMEM, "cudaMallocHost: %s", cudaGetErrorString(e));
+        }
+        for (int j = 0; j < 2; j++) CUDA_TRY(cudaEventCreateWithFlags(&dom->ltsCtlReady[j], cudaEventDisableTiming));
+    }
     LtsControl c{};
     CUDA_TRY(cudaMemcpyAsync(&c, dom->dLtsCtl, sizeof(LtsControl), cudaMemcpyDeviceToHost, dom->stream));
     CUDA_TRY(cudaStreamSynchronize(dom->stream));
@@ -1540,11 +1555,30 @@ int swe_gpu_lts_advance(swe_gpu_domain *dom, float t_end, int max_iterations, in
     const int limit = int(std::min<long long>(INT32_MAX, (long long)c.iterations + max_iterations));
     CUDA_TRY(cudaMemcpyAsync(&dom->dLtsCtl->target, &t_end, sizeof(float), cudaMemcpyHostToDevice, dom->stream));
     CUDA_TRY(cudaMemcpyAsync(&dom->dLtsCtl->iterLimit, &limit, sizeof(int), cudaMemcpyHostToDevice, dom->stream));
-    while (c.t < t_end && c.iterations < limit) {
+    // replays of `batch` iterations with the next one queued before the
+    // host reads the last one's control block: the device does not wait for
+    // the host between replays.  Iterations queued past the target or the
+    // limit do nothing (the kernels test the control block).
+    auto replay = [&](int slot) -> int {
         CUDA_TRY(cudaGraphLaunch(dom->ltsGraph, dom->stream));
         dom->launches += dom->ltsGraphKernels;
-        CUDA_TRY(cudaMemcpyAsync(&c, dom->dLtsCtl, sizeof(LtsControl), cudaMemcpyDeviceToHost, dom->stream));
+        CUDA_TRY(cudaMemcpyAsync(dom->ltsCtlHost + slot, dom->dLtsCtl, sizeof(LtsControl), cudaMemcpyDeviceToHost,
+                                 dom->stream));
+        CUDA_TRY(cudaEventRecord(dom->ltsCtlReady[slot], dom->stream));
+        return SWE_GPU_OK;
+    };
+    if (c.t < t_end && c.iterations < limit) {
+        int rc = replay(0);
+        if (rc) return rc;
+        for (int slot = 0;; slot ^= 1) {
+            rc = replay(slot ^ 1);
+            if (rc) return rc;
+            CUDA_TRY(cudaEventSynchronize(dom->ltsCtlReady[slot]));
+            c = dom->ltsCtlHost[slot];
+            if (!(c.t < t_end && c.iterations < limit)) break;
+        }
         CUDA_TRY(cudaStreamSynchronize(dom->stream));
+        c = dom->ltsCtlHost[0].iterations > dom->ltsCtlHost[1].iterations ? dom->ltsCtlHost[0] : dom->ltsCtlHost[1];
     }
     // the update passes push no ghosts: a check with the run over carries the
     // last ring into the current buffer, as the reference's single array holds it
