@@ -870,6 +870,29 @@ def surrogate_fp64_proxy(swe, m, device, n=512, duration=300.0):
     return out
 
 
+def profile_lts(seconds):
+    """small case for launch lists of local time stepping: the bench's lts
+    workload (shoreline ramp 2048^2 as 8x8 blocks of 256^2, HLLE, 1 s
+    intervals), one warm-up interval, then `seconds` intervals"""
+    import swe_gb300 as swe
+    n, nb = 2048, 64
+    geo, h, hu, hv, b = swe.init_domain(swe.SCENARIO_SHORELINE, n, n, nb, [SEED, 50000.0])
+    D = swe.Domain(geo["nx_cols"], geo["ny_rows"], geo["dx"], geo["dy"], boundary=geo["boundary"], solver=swe.HLLE,
+                   lts_max_timestep=1.0, duration=200.0)
+    D.upload(h, hu, hv, b)
+    D.exchange_bathymetry()
+    D.lts_advance(1.0)
+    _, _, it0, _ = D.lts_state()
+    t0 = time.perf_counter()
+    done, _ = D.lts_advance(1.0 + seconds)
+    el = time.perf_counter() - t0
+    _, _, it1, _ = D.lts_state()
+    log("lts intervals", done, "inner iterations", it1 - it0, "us per iteration", 1e6 * el / max(1, it1 - it0),
+        "device status", D.status())
+    D.close()
+    return 0
+
+
 def profile_surrogate(n):
     """small case for captures of the surrogate kernels: the shoreline ramp on
     one n x n block, a surrogate trained for 3 epochs on every 8th wet edge of
@@ -1100,9 +1123,13 @@ def main():
                     help="solver of the --profile run (the bench itself always runs HLLE)")
     ap.add_argument("--profile-surrogate", type=int, default=0, metavar="N",
                     help="only the surrogate step on an N x N shoreline (for ncu captures)")
+    ap.add_argument("--profile-lts", type=float, default=0.0, metavar="SECONDS",
+                    help="only local time stepping, SECONDS simulated after a warm-up interval (for ncu captures)")
     args = ap.parse_args()
     if args.profile_surrogate:
         return profile_surrogate(args.profile_surrogate)
+    if args.profile_lts > 0:
+        return profile_lts(args.profile_lts)
     world, rank, local = dist_init()
     if args.impl == "reference":
         rc = run_reference(args, world, rank)

@@ -120,6 +120,8 @@ struct __align__(128) GroupState {
     int unitsFast;           // segments of the fast-arithmetic step in this group
     int ringStale;           // local time stepping: the update flipped the buffers; the
                              // current buffer's ghost ring is still in the other one
+    int ltsStep;             // local time stepping, set by the check: 0 when the block is at
+                             // the start of its interval, else its stepSize
 };
 
 // Bound tile of the bounded speed pass: 32 x 32 interior cells of a block,

@@ -234,20 +234,18 @@ __global__ void ltsCheckKernel(const DomainDev d) {
             }
             if (ltsInSync(L) && L.stepSizeCounter < L.stepSize) L.stepSizeCounter++;
             G->enabled = ltsInSync(L) ? 1 : 0;
+            G->ltsStep = L.stepSizeCounter <= 0 ? 0 : L.stepSize;
         } else {
             G->enabled = 0;
         }
     }
-    // the block's state back to global memory
+    // the block's state back to global memory (read by the next kernels
+    // only); the last CTA lists the enabled blocks (update pass) and those at
+    // the start of their interval (speed pass) from what thread 0 wrote
+    // before its release; the others take Tsync / stepSize, the step the
+    // speed pass would round to (SWE_Block::getRoundTimestep)
     __syncthreads();
-    if (running && t < kLInts) {
-        reinterpret_cast<int *>(d.lts + k)[t] = reinterpret_cast<const int *>(&L)[t];
-        __threadfence();
-    }
-    // the last CTA lists the enabled blocks (update pass) and those at the
-    // start of their interval (speed pass); the others take Tsync / stepSize,
-    // the step the speed pass would round to (SWE_Block::getRoundTimestep)
-    __syncthreads();
+    if (running && t < kLInts) reinterpret_cast<int *>(d.lts + k)[t] = reinterpret_cast<const int *>(&L)[t];
     if (t == 0)
         sLast = arriveAcqRel(reinterpret_cast<unsigned *>(d.ltsWork + kLwArrCheck), 1u) + 1u == gridDim.x;
     __syncthreads();
@@ -258,20 +256,22 @@ __global__ void ltsCheckKernel(const DomainDev d) {
         const int nb = d.nblocks, TY = d.tileRows, T = blockDim.x, i = threadIdx.x;
         const int chunk = (nb + T - 1) / T;
         const int j0 = min(nb, i * chunk), j1 = min(nb, j0 + chunk);
-        auto entry = [&](int j, int &pairs, bool &upd, bool &spd) {
+        auto entry = [&](int j, int &pairs, bool &upd, bool &spd, int &step) {
             const BlockDesc &Bj = d.blocks[j];
+            const int en = __ldcg(&d.groups[j].enabled);  // one round: independent loads
+            step = __ldcg(&d.groups[j].ltsStep);
             pairs = ((Bj.ny + TY - 1) / TY) * Bj.nx;
-            upd = __ldcg(&d.groups[j].enabled) != 0;
-            spd = upd && __ldcg(&d.lts[j].stepSizeCounter) <= 0;
+            upd = en != 0;
+            spd = upd && step == 0;
         };
         int v[4] = {0, 0, 0, 0};  // enabled blocks, their pairs, interval starts, their pairs
         constexpr int kCache = 4;  // the first entries' values, kept for the second pass
         int cPairs[kCache];
         bool cUpd[kCache], cSpd[kCache];
         for (int j = j0; j < j1; j++) {
-            int pairs;
+            int pairs, step;
             bool upd, spd;
-            entry(j, pairs, upd, spd);
+            entry(j, pairs, upd, spd, step);
             if (j - j0 < kCache) {
                 cPairs[j - j0] = pairs;
                 cUpd[j - j0] = upd;
@@ -285,7 +285,7 @@ __global__ void ltsCheckKernel(const DomainDev d) {
                 v[2]++;
                 v[3] += pairs;
             } else if (upd) {
-                d.groups[j].dt = C.maxTimestepLocal / float(__ldcg(&d.lts[j].stepSize));
+                d.groups[j].dt = C.maxTimestepLocal / float(step);
             }
         }
         // exclusive scans of the four counts over the CTA: within each warp
@@ -317,14 +317,14 @@ __global__ void ltsCheckKernel(const DomainDev d) {
         int *lU = lwList(W, nb, true), *pU = lwPrefix(W, nb, true);
         int *lS = lwList(W, nb, false), *pS = lwPrefix(W, nb, false);
         for (int j = j0; j < j1; j++) {
-            int pairs;
+            int pairs, step;
             bool upd, spd;
             if (j - j0 < kCache) {
                 pairs = cPairs[j - j0];
                 upd = cUpd[j - j0];
                 spd = cSpd[j - j0];
             } else {
-                entry(j, pairs, upd, spd);
+                entry(j, pairs, upd, spd, step);
             }
             if (upd) {
                 pU[o[0]] = o[1];
