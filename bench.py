@@ -307,10 +307,11 @@ def reference_binary():
     return None
 
 
-def reference_run(binary, duration, blocks=N_BLOCKS, cells=N_CELLS_SIDE):
+def reference_run(binary, duration, blocks=N_BLOCKS, cells=N_CELLS_SIDE, lts=0.0):
     """One run of the stock driver at cells^2 over `blocks` blocks for
-    `duration` simulated seconds on every host core; returns (cell-updates,
-    wall seconds).  Cell-updates come from the driver's own log (FLOP_COUNT /
+    `duration` simulated seconds on every host core (lts > 0: local time
+    stepping with intervals of `lts` s, its -l); returns (cell-updates, wall
+    seconds).  Cell-updates come from the driver's own log (FLOP_COUNT /
     270, src/tools/Collector.hpp:129-142, 270 flop per cell-update at
     src/blocks/SWE_DimensionalSplittingMpi.cpp:458).  Its WALL_TIME column is
     not usable: the driver folds the blocks' collectors into its own with a
@@ -324,7 +325,8 @@ def reference_run(binary, duration, blocks=N_BLOCKS, cells=N_CELLS_SIDE):
         env = dict(os.environ, OMP_NUM_THREADS=str(cores))
         t0 = time.perf_counter()
         r = subprocess.run([binary, "-x", str(cells), "-y", str(cells), "-b", str(blocks), "-t", repr(float(duration)),
-                            "-n", "1", "-o", base, "-w", "0", "-l", "0"], capture_output=True, text=True, env=env,
+                            "-n", "1", "-o", base, "-w", "0", "-l", repr(float(lts))], capture_output=True, text=True,
+                           env=env,
                            cwd=tmp)
         el = time.perf_counter() - t0
         if r.returncode != 0:
@@ -789,6 +791,7 @@ def surrogate_measure(swe, device, steps=10, err_steps=120):
             errs[k] = float(np.abs(ends[k][1] - ref).sum() / cells)
     D.close()
     fp64 = surrogate_fp64_proxy(swe, m, device)
+    batched = ensemble_surrogate_measure(swe, m, device, stream)
     m.close()
     flop_edge = 2 * (6 * 64 + 2 * 64 * 64 + 64 * 4)
     return {"workload": "surrogate of the augmented solver, shoreline ramp 4096x4096 as 4x4 blocks of 1024^2, unsplit",
@@ -798,9 +801,74 @@ def surrogate_measure(swe, device, steps=10, err_steps=120):
             "mlp_flop_per_edge": flop_edge,
             "mlp_tflops_over_step": nedges * flop_edge / (1e-3 * ms_sur) / 1e12,
             "l1_error_per_cell_vs_augmented": errs, "error_steps": err_steps, "fp64_proxy": fp64,
+            "batched": batched,
             "training": {"edges": int(E.shape[1]), "epochs": epochs, "batch": 8192, "seconds": train_s,
                          "edges_per_s": epochs * E.shape[1] / train_s, "loss_first_epoch": float(losses[0]),
                          "loss_last_epoch": float(losses[-1])}}
+
+
+def ensemble_surrogate_measure(swe, m, device, stream, steps=10, err_steps=100, count=256):
+    """The batched + surrogate form: the ensemble workload (256 radial dam
+    breaks, nx, ny in 64..1024, b = 0, one seed) with the augmented solver
+    in one handle, stepped by the surrogate (swe_gpu_surrogate_step on the
+    ensemble) against the augmented solver's own batched step.  Timed like
+    the single-domain rates (CUDA events, `steps` steps after 3 warm-up
+    steps).  Accuracy: after err_steps steps (each instance at its own dt),
+    the relative L1 distance of h to the augmented solver's batched run,
+    largest and median over the instances."""
+    import torch
+    inst, states = swe.dam_break_ensemble(count, seed=SEED)
+    cells = float(sum(nx * ny for nx, ny, *_ in inst))
+
+    def make():
+        E = swe.Ensemble(inst, solver=swe.AUGRIE, device=device)
+        E.set_stream(stream.cuda_stream)
+        E.upload(*[np.concatenate([st[i] for st in states]) for i in range(4)])
+        E.exchange_bathymetry()
+        return E
+
+    def timed(E, fn):
+        fn(E, 3)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            fn(E, steps)
+            e1.record(stream)
+        stream.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    rates = {}
+    E = make()
+    rates["augmented_ensemble_step"] = cells / (1e-3 * timed(E, lambda E, k: E.step(k)))
+    E.close()
+    E = make()
+    rates["surrogate_ensemble_step"] = cells / (1e-3 * timed(E, lambda E, k: E.surrogate_step(m, k, count=False)))
+    used = E.surrogate_step(m, 1)
+    nedges = E.surrogate_edge_count()
+    E.close()
+    h = {}
+    status = 0
+    for name in ("augmented", "surrogate"):
+        E = make()
+        if name == "surrogate":
+            E.surrogate_step(m, err_steps, count=False)
+        else:
+            E.step(err_steps)
+        h[name] = E.download()[0].astype(np.float64)
+        status |= E.status()
+        E.close()
+    offs = np.cumsum([0] + [(nx + 2) * (ny + 2) for nx, ny, *_ in inst])
+    rel = []
+    for k, (nx, ny, *_) in enumerate(inst):
+        a = h["augmented"][offs[k]:offs[k + 1]].reshape(nx + 2, ny + 2)[1:-1, 1:-1]
+        b_ = h["surrogate"][offs[k]:offs[k + 1]].reshape(nx + 2, ny + 2)[1:-1, 1:-1]
+        rel.append(float(np.abs(b_ - a).sum() / np.abs(a).sum()))
+    return {"workload": "%d radial dam breaks, nx, ny in 64..1024, augmented solver, unsplit, own dt each" % count,
+            "unit": "cell-updates/s (sum over instances)", "cells": int(cells), "rates": rates,
+            "speedup_vs_augmented_ensemble_step": rates["surrogate_ensemble_step"] / rates["augmented_ensemble_step"],
+            "surrogate_edge_fraction": used / nedges, "error_steps": err_steps,
+            "rel_l1_h_vs_augmented_max": max(rel), "rel_l1_h_vs_augmented_median": float(np.median(rel)),
+            "device_status": status}
 
 
 def surrogate_fp64_proxy(swe, m, device, n=512, duration=300.0):
@@ -918,6 +986,24 @@ def profile_surrogate(n):
     D.close()
     m.close()
     return 0
+
+
+def reference_lts_rate():
+    """The reference's own local time stepping on the host cores at the
+    shape of the lts workload: the stock overdecomposed driver at 2048^2 as
+    8 x 8 blocks with 1 s intervals (-b 64 -l 1) on its own scenario (the
+    radial-bathymetry dam break, HLLE).  A run always completes whole
+    intervals, so the rate is the difference of a 2 s and a 1 s run."""
+    binary = reference_binary()
+    if not binary:
+        return None
+    cores, model = host_cpu()
+    u1, w1 = reference_run(binary, 1.0, blocks=64, lts=1.0)
+    u2, w2 = reference_run(binary, 2.0, blocks=64, lts=1.0)
+    return {"value": (u2 - u1) / max(w2 - w1, 1e-6), "unit": "cell-updates/s (its log's FLOP_COUNT / 270)",
+            "cores": cores, "cpu_model": model, "kind": "reference",
+            "sample": "stock swe_benchmark_mpioverdecomp -x 2048 -y 2048 -b 64 -l 1 (its radial-bathymetry dam "
+                      "break, HLLE), the second 1 s interval: a -t 2 run minus a -t 1 run, %d OpenMP threads" % cores}
 
 
 def cpu_reference_baseline(args):
@@ -1068,6 +1154,11 @@ def run_gb300(args, world, rank, local):
     split = split_measure(swe, local) if rank == 0 else None
     drivers = drivers_measure() if rank == 0 else None
     base = cpu_reference_baseline(args) if rank == 0 else None
+    if rank == 0:
+        try:
+            lts["cpu_reference"] = reference_lts_rate()
+        except Exception as e:
+            log("reference lts run failed:", e)
     clocks = clk.summary()
     issue = None
     if warp_inst and clocks.get("sm_mhz"):

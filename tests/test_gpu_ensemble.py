@@ -116,3 +116,58 @@ def test_ensemble_of_split_steps(swe):
         ref, _ = alone(swe, inst[k], states[k], 3, 10, semantics=1)
         for a, b_, name in zip(blk, ref, "h hu hv b".split()):
             assert_bitwise(a, b_, "instance %d %s" % (k, name))
+
+
+def test_ensemble_surrogate_step_equals_instances_alone(swe):
+    """The batched + surrogate form: an augmented-solver ensemble stepped by
+    the MLP surrogate (swe_gpu_surrogate_step on the ensemble handle) is,
+    instance by instance, bit-identical to each simulation's own surrogate
+    run; without a network the same call is the ensemble's augmented step."""
+    inst, states = swe.dam_break_ensemble(6, seed=7, sizes=np.arange(64, 193, 32))
+    nx, ny, dx, dy, bnd = inst[0]
+    A = swe.Domain([nx], [ny], dx, dy, boundary=bnd, solver=swe.AUGRIE)
+    A.upload(*states[0])
+    A.exchange_bathymetry()
+    A.step(4)
+    e, tg = A.log_edges(stride=1, capacity=1 << 18)
+    A.close()
+    m = swe.Surrogate(seed=3)
+    m.train(e, tg, epochs=4, batch=2048, lr=2e-3, seed=3)
+    nsteps = 12
+
+    def batched(model, plain=False):
+        E = swe.Ensemble(inst, solver=swe.AUGRIE)
+        E.upload(*[np.concatenate([s[i] for s in states]) for i in range(4)])
+        E.exchange_bathymetry()
+        used = 0
+        if plain:
+            E.step(nsteps)
+        else:
+            used = E.surrogate_step(model, nsteps)
+        out = E.download()
+        t, dt, steps = E.group_state()
+        assert E.status() == 0
+        E.close()
+        return out, t, used
+
+    out, t, used = batched(m)
+    assert used > 0
+    for k, blk in enumerate(split_blocks(out, inst)):
+        nx, ny, dx, dy, bnd = inst[k]
+        D = swe.Domain([nx], [ny], dx, dy, boundary=bnd, solver=swe.AUGRIE)
+        D.upload(*states[k])
+        D.exchange_bathymetry()
+        D.surrogate_step(m, nsteps)
+        ref = D.download()
+        tref, _ = D.time()
+        assert D.status() == 0
+        D.close()
+        assert np.float32(t[k]) == np.float32(tref), "instance %d clock" % k
+        for a, b_, name in zip(blk, ref, "h hu hv b".split()):
+            assert_bitwise(a, b_, "instance %d %s" % (k, name))
+    m.close()
+    out0, t0, _ = batched(None)
+    out1, t1, _ = batched(None, plain=True)
+    assert_bitwise(np.asarray(t0, np.float32), np.asarray(t1, np.float32), "clocks")
+    for a, b_, name in zip(out0, out1, "h hu hv b".split()):
+        assert_bitwise(a, b_, name)
