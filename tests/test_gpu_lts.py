@@ -75,6 +75,48 @@ def test_lts_last_interval_reaches_duration(swe, oracle_mod):
     assert_bitwise(hv, ref[2], "hv")
 
 
+def test_lts_iteration_budget_resumes_bitwise(swe, oracle_mod):
+    """swe_gpu_lts_advance with a budget of 2 inner iterations per call: each
+    call stops at the budget (graph replays queued past it do nothing) and
+    carries the ghost ring into the current buffer; the next call resumes.
+    Every interval takes the oracle's number of inner iterations in
+    ceil(iterations / 2) calls, and two intervals run that way give the
+    oracle's step counts and state bit for bit."""
+    budget = 2
+    geo, h, hu, hv, b = swe.init_domain(swe.SCENARIO_SHORELINE, 128, 96, 16, [11, 50000.0])
+    R = oracle_mod.Domain(geo["nx_cols"], geo["ny_rows"], geo["dx"], geo["dy"], outer=geo["boundary"], solver=4,
+                          lts_max_timestep=1.0, duration=40.0)
+    R.set_state(h, hu, hv, b)
+    R.bathymetry_ghosts()
+    D = swe.Domain(geo["nx_cols"], geo["ny_rows"], geo["dx"], geo["dy"], boundary=geo["boundary"], solver=4,
+                   lts_max_timestep=1.0, duration=40.0)
+    D.upload(h, hu, hv, b)
+    D.exchange_bathymetry()
+    for i in range(2):
+        it, rsteps = R.lts_interval()
+        assert it > budget
+        _, _, start, _ = D.lts_state()
+        calls = 0
+        while True:
+            _, _, it0, _ = D.lts_state()
+            D.lts_advance(i + 0.5, max_iterations=budget)
+            _, nint, it1, steps = D.lts_state()
+            calls += 1
+            if nint == i + 1:
+                assert 0 < it1 - it0 <= budget
+                break
+            assert it1 - it0 == budget and calls < 100
+        assert it1 - start == it, "inner iterations of interval %d" % i
+        assert calls == -(-it // budget)
+        assert_bitwise(steps, rsteps.astype(np.int32), "block step counts, interval %d" % i)
+    out = D.download()
+    assert D.status() == 0
+    D.close()
+    ref = R.get_state()
+    for a, r, name in zip(out, ref, "h hu hv".split()):
+        assert_bitwise(a, r, name)
+
+
 def test_lts_domain_refuses_global_steps(swe):
     geo, h, hu, hv, b = swe.init_domain(swe.SCENARIO_SHORELINE, 64, 64, 4, [11, 50000.0])
     D = swe.Domain(geo["nx_cols"], geo["ny_rows"], geo["dx"], geo["dy"], boundary=geo["boundary"], solver=4,
