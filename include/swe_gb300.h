@@ -218,8 +218,10 @@ int swe_gpu_block_steps(swe_gpu_domain *dom, long long *steps);
  * the interval, with time-interpolated ghost layers (src/blocks/SWE_Block.hh:311-562,
  * src/examples/swe_mpi_overdecomp.cpp:266-343), until the interval start time
  * t reaches t_end or max_iterations inner iterations ran.  The iterations are
- * decided on the device and replayed from a captured graph; the host reads
- * the control block once per batch.  Returns the finished intervals and t;
+ * decided on the device and replayed from a captured graph of 8; the next
+ * replay is queued before the host reads the last one's control block, and
+ * iterations past t_end or the limit do nothing.  Returns the finished
+ * intervals and t;
  * SWE_GPU_INCOMPLETE when exactly max_iterations inner iterations ran first. */
 int swe_gpu_lts_advance(swe_gpu_domain *dom, float t_end, int max_iterations, int *intervals_done, float *t_now);
 /* Local time stepping counters: t, finished intervals, inner iterations and,
