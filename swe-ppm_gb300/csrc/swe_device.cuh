@@ -53,7 +53,7 @@ struct BlockDesc {
 };
 
 // Per-block state of local time stepping (src/blocks/SWE_Block.hh:214-229).
-struct LtsBlock {
+struct __align__(16) LtsBlock {
     int received[4];          // GhostlayerState per side
     float borderTimestep[4];  // the neighbour's total local time when its layer was received
     int stepSize, stepSizeCounter, timestepCounter, notified;

@@ -29,6 +29,8 @@
 // column later, when its right edge is known.
 #pragma once
 
+#include <cstddef>
+
 #include "swe_device.cuh"
 
 namespace swegb {
@@ -156,7 +158,8 @@ __device__ __forceinline__ bool ltsInSync(const LtsBlock &L) {
 /// (DomainDev::ltsWork) names the blocks that take part, with the prefix sums
 /// of their (row tile, column) pairs; CTA c takes pairs [total c / grid,
 /// total (c+1) / grid), cut at tile ends and every kMaxTileCols columns.
-/// segment(unit, pairs, block's pairs) runs each piece.
+/// segment(unit, pairs, block's pairs) runs each piece.  Called by every
+/// thread of the CTA.
 template <bool UPDATE, class Seg>
 __device__ __forceinline__ void ltsSegments(const DomainDev &d, int TY, Seg &&segment) {
     int *W = d.ltsWork;
@@ -167,24 +170,37 @@ __device__ __forceinline__ void ltsSegments(const DomainDev &d, int TY, Seg &&se
     long long pos = total * blockIdx.x / gridDim.x;
     const long long end = total * (blockIdx.x + 1) / gridDim.x;
     if (pos >= end || n <= 0) return;
-    int lo = 0, hi = n - 1;  // the entry holding pair pos: pref[j] <= pos < pref[j+1]
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) / 2;
-        if (__ldcg(pref + mid) <= pos) lo = mid;
-        else hi = mid - 1;
+    // the entry holding pair pos, pref[j] <= pos < pref[j+1], with its block
+    // and prefixes: every thread tests its own entries, so the search is one
+    // round of loads (a binary search is log2(n) dependent ones)
+    __shared__ int sJ, sK, sP0, sP1;
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int a = __ldcg(pref + i), b = __ldcg(pref + i + 1), k = __ldcg(list + i);
+        if (a <= pos && pos < b) {
+            sJ = i;
+            sK = k;
+            sP0 = a;
+            sP1 = b;
+        }
     }
-    int j = lo;
+    __syncthreads();
+    int j = sJ, k = sK, p0 = sP0, p1 = sP1;
     while (pos < end) {
-        const int k = __ldcg(list + j);
         const BlockDesc &B = d.blocks[k];
-        const long long local = pos - __ldcg(pref + j);
+        const long long local = pos - p0;
         const int nx = B.nx;
         const int tile = int(local / nx), col = int(local % nx) + 1;
         const int len = int(min((long long)min(nx + 1 - col, kMaxTileCols), end - pos));
         const int tiles = (B.ny + TY - 1) / TY;
         segment(WorkUnit{k, 1 + tile * TY, col, col + len}, unsigned(len), unsigned(tiles * nx));
         pos += len;
-        if (pos >= __ldcg(pref + j + 1)) ++j;
+        if (pos >= p1 && pos < end) {  // the next entry
+            ++j;
+            k = __ldcg(list + j);
+            p0 = p1;
+            p1 = __ldcg(pref + j + 1);
+        }
     }
 }
 
@@ -194,26 +210,54 @@ __device__ __forceinline__ void ltsSegments(const DomainDev &d, int TY, Seg &&se
 /// counters reset (src/examples/swe_mpi_overdecomp.cpp:332-342).  Every
 /// block's total local time is published for the next iteration's exchange.
 __device__ __forceinline__ void ltsEndIteration(const DomainDev &d) {
+    static_assert(sizeof(LtsBlock) == 64 && offsetof(LtsBlock, stepSize) == 32 && alignof(LtsBlock) >= 16,
+                  "LtsBlock as four int4");
     LtsControl &C = *d.ltsCtl;
     const bool running = ltsRunning(C);
+    // each block's ghost-layer states and counters in one load round (the
+    // first kCache blocks of a thread stay in registers between the passes)
+    constexpr int kCache = 4;
+    int4 rec[kCache], cnt[kCache];  // received[4]; stepSize, stepSizeCounter, timestepCounter, notified
+    auto load = [&](int k, int4 &r, int4 &c) {
+        const int4 *p = reinterpret_cast<const int4 *>(d.lts + k);
+        r = p[0];
+        c = p[2];
+    };
+    auto finished = [](const int4 &r, const int4 &c) {
+        const bool inSync = r.x != GL_UNVALID && r.y != GL_UNVALID && r.z != GL_UNVALID && r.w != GL_UNVALID &&
+                            c.y <= c.x;
+        return (c.y >= c.x && inSync) || c.w != 0;
+    };
     bool done = true;
-    if (running)
-        for (int k = threadIdx.x; k < d.nblocks; k += blockDim.x) {
-            const LtsBlock &L = d.lts[k];
-            if (!((L.stepSizeCounter >= L.stepSize && ltsInSync(L)) || L.notified)) done = false;
+    for (int j = 0, k = threadIdx.x; k < d.nblocks; j++, k += blockDim.x) {
+        int4 r, c;
+        load(k, r, c);
+        if (j < kCache) {
+            rec[j] = r;
+            cnt[j] = c;
         }
-    done = __syncthreads_and(done);
-    if (running && done) {
-        for (int k = threadIdx.x; k < d.nblocks; k += blockDim.x) {
-            LtsBlock &L = d.lts[k];
-            L.lastStepSize = L.stepSize;
-            L.stepSizeCounter = 0;
-            L.stepSize = 0;
-            L.timestepCounter++;
-        }
+        if (running && !finished(r, c)) done = false;
     }
-    __syncthreads();
-    for (int k = threadIdx.x; k < d.nblocks; k += blockDim.x) d.ltsLocal[k] = ltsTotalLocal(d.lts[k], C);
+    done = __syncthreads_and(done);
+    for (int j = 0, k = threadIdx.x; k < d.nblocks; j++, k += blockDim.x) {
+        int4 r, c;
+        if (j < kCache) {
+            c = cnt[j];
+        } else {
+            load(k, r, c);
+        }
+        if (running && done) {
+            int *L = reinterpret_cast<int *>(d.lts + k);
+            L[offsetof(LtsBlock, lastStepSize) / 4] = c.x;
+            c = make_int4(0, 0, c.z + 1, c.w);
+            reinterpret_cast<int4 *>(d.lts + k)[2] = c;
+        }
+        LtsBlock T{};
+        T.stepSize = c.x;
+        T.stepSizeCounter = c.y;
+        T.timestepCounter = c.z;
+        d.ltsLocal[k] = ltsTotalLocal(T, C);
+    }
     if (threadIdx.x == 0 && running) {
         C.iterations++;
         if (done) {
