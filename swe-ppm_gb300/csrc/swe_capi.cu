@@ -458,13 +458,16 @@ int enqueueStep(swe_gpu_domain *D) {
 }
 
 /// one inner iteration of local time stepping (see swe_lts.cu): check
-/// (with the exchange), speed pass of the blocks at an interval start,
-/// update pass of the enabled blocks (with the iteration's end)
+/// (with the exchange), speed pass of the blocks at an interval start
+/// (unless the check runs it, DomainDev::ltsCheckSpeed), update pass of the
+/// enabled blocks (with the iteration's end)
 int enqueueLtsIteration(swe_gpu_domain *D) {
     CUDA_TRY(launchLtsCheck(D->dev, D->stream));
     D->launches++;
-    int rc = enqueueSpeed(D);
-    if (rc) return rc;
+    if (!D->dev.ltsCheckSpeed) {  // (else the check computed the interval starts' dt)
+        int rc = enqueueSpeed(D);
+        if (rc) return rc;
+    }
     return enqueueUpdate(D);
 }
 
@@ -1009,6 +1012,12 @@ int buildDomain(const std::vector<BlockSpec> &spec, const DomainOptions &o, swe_
     D->dev.ltsCtl = D->dLtsCtl;
     D->dev.ltsWork = D->dLtsWork;
     D->dev.ltsLocal = D->dLtsLocal;
+    {
+        long long maxCells = 0;
+        for (const BlockDesc &B : D->blocks) maxCells = std::max(maxCells, (long long)B.nx * B.ny);
+        D->dev.ltsCheckSpeed = D->lts && (D->solver == SOLVER_FWAVE || D->solver == SOLVER_HLLE) &&
+                               maxCells <= kLtsCheckSpeedCells;
+    }
     for (int f = 0; f < 3; f++) D->dev.ring[f] = D->dRing[f];
     D->dev.tileW = D->dTileW;
     D->dev.tileKey = D->dTileKey;

@@ -169,7 +169,18 @@ struct DomainDev {
     float *ring[3];                  // receive rings of h, hu, hv
     int *ltsWork;                    // the iteration's work lists (layout: kLw* below)
     float *ltsLocal;                 // every block's total local time at the end of the last iteration
+    int ltsCheckSpeed;               // 1: the check computes an interval start's dt itself
+                                     // (f-wave / HLLE, blocks up to kLtsCheckSpeedCells cells)
 };
+
+// Largest block whose interval-start speed pass the check kernel's one CTA
+// runs itself (128^2 cells); larger blocks keep the grid-wide speed pass.
+// The separate pass costs a launch in every inner iteration, the check's
+// one CTA a block-sized speed pass on one SM in the first iteration of an
+// interval: on 8 x 8 blocks at 16 to 32 steps per interval the check won at
+// 128^2 blocks (1024^2: 40.2 -> 38.4 us per iteration) and lost at 256^2
+// (2048^2: 74.9 -> 76.5 us).
+constexpr long long kLtsCheckSpeedCells = 128LL * 128LL;
 
 // Work lists of a local-time-stepping iteration (DomainDev::ltsWork, ints),
 // built by the last CTA of the check kernel: the enabled blocks (update pass)

@@ -15,7 +15,10 @@
 //                   iteration iff its layers are in sync (GroupState::enabled).
 //                   The kernel's last CTA lists the enabled blocks and those
 //                   at the start of their interval (DomainDev::ltsWork), and
-//                   gives the others their step Tsync / stepSize.
+//                   gives the others their step Tsync / stepSize.  For the
+//                   f-wave and HLLE solvers on blocks of up to 128^2 cells
+//                   the CTA of a block at the start of its interval runs the
+//                   block's speed pass itself and there is no speed launch.
 //   speed pass      the blocks at the start of an interval: maxTimestep
 //                   rounded to Tsync / 2^k (within an interval the step does
 //                   not depend on the wave speed)
@@ -74,6 +77,53 @@ __device__ __forceinline__ void perimeterIndex(const BlockDesc &B, int i, int &s
     else { side = 3; pos = i - 2 * ny - nx + 1; }
 }
 
+/// The block's speed pass by one CTA (computeNumericalFluxes' maximum wave
+/// speed, src/blocks/SWE_DimensionalSplittingMpi.cpp:391-446): every x-edge
+/// (x-1|x), x = 1..nx+1, of rows 1..ny and every y-edge (y-1|y), y =
+/// 1..ny+1, of columns 1..nx, with the speed pass's cell quantities and edge
+/// speeds; returns the thread's maximum.  Threads take rows (consecutive
+/// threads, consecutive rows) and march along x through one of up to
+/// blockDim / ny column ranges.
+template <int S> __device__ float blockEdgeSpeed(const DomainDev &d, const BlockDesc &B, int cur) {
+    const float *H = pick(d.h, cur) + B.base, *HU = pick(d.hu, cur) + B.base, *HV = pick(d.hv, cur) + B.base;
+    const float *BT = d.b + B.base;
+    const size_t P = size_t(B.pitch);
+    const int T = blockDim.x, t = threadIdx.x;
+    const int rt = min(B.ny, T), ng = min(T / rt, B.nx);
+    float smax = 0.f;
+    if (t >= rt * ng) return smax;
+    const int g = t / rt;
+    const int xa = 1 + int((long long)B.nx * g / ng), xb = int((long long)B.nx * (g + 1) / ng);
+    for (int y = 1 + t % rt; y <= B.ny; y += rt) {
+        Cell px, dummy;
+        {
+            const size_t o = size_t(xa - 1) * P + y;
+            cellQuantities<S>(H[o], HU[o], HV[o], BT[o], px, dummy);
+        }
+        for (int x = xa; x <= xb; x++) {
+            const size_t o = size_t(x) * P + y;
+            Cell cx, cy, bx, by;
+            cellQuantities<S>(H[o], HU[o], HV[o], BT[o], cx, cy);
+            cellQuantities<S>(H[o - 1], HU[o - 1], HV[o - 1], BT[o - 1], bx, by);
+            smax = vmax(smax, edgeSpeed<S>(px, cx));  // (x-1|x)
+            smax = vmax(smax, edgeSpeed<S>(by, cy));  // (y-1|y)
+            if (y == B.ny) {                           // (ny|ny+1)
+                Cell ax, ay;
+                cellQuantities<S>(H[o + 1], HU[o + 1], HV[o + 1], BT[o + 1], ax, ay);
+                smax = vmax(smax, edgeSpeed<S>(cy, ay));
+            }
+            px = cx;
+        }
+        if (xb == B.nx) {  // (nx|nx+1)
+            const size_t o = size_t(B.nx + 1) * P + y;
+            Cell gx, gy;
+            cellQuantities<S>(H[o], HU[o], HV[o], BT[o], gx, gy);
+            smax = vmax(smax, edgeSpeed<S>(px, gx));
+        }
+    }
+    return smax;
+}
+
 /// exchangeGhosts + checkAllGhostlayers (src/blocks/SWE_Block.hh:375-436):
 /// one CTA per block; the last CTA lists the iteration's work
 __global__ void ltsCheckKernel(const DomainDev d) {
@@ -84,7 +134,8 @@ __global__ void ltsCheckKernel(const DomainDev d) {
     __shared__ int sLast;
     __shared__ int sScan[4][kLtsCheckThreads / 32];
     __shared__ LtsBlock L;   // the block's state, staged: its reads and writes stay on chip
-    __shared__ int sCur, sStale;
+    __shared__ int sCur, sStale, sSpeed;
+    __shared__ float sRed[kLtsCheckThreads / 32];
     static_assert(sizeof(LtsBlock) % 4 == 0 && sizeof(LtsBlock) / 4 + 2 <= 32, "staging by warp 0");
     static_assert(kLtsCheckThreads % 32 == 0 && kLtsCheckThreads <= 1024, "warp scan");
     pdlWaitAndRelease();
@@ -235,16 +286,31 @@ __global__ void ltsCheckKernel(const DomainDev d) {
             if (ltsInSync(L) && L.stepSizeCounter < L.stepSize) L.stepSizeCounter++;
             G->enabled = ltsInSync(L) ? 1 : 0;
             G->ltsStep = L.stepSizeCounter <= 0 ? 0 : L.stepSize;
+            sSpeed = d.ltsCheckSpeed && ltsInSync(L) && L.stepSizeCounter <= 0;
         } else {
             G->enabled = 0;
+            sSpeed = 0;
         }
+    }
+    __syncthreads();
+    if (sSpeed) {
+        // the block starts its interval: its speed pass and getRoundTimestep
+        // here, on the ghost ring just set (f-wave / HLLE, small blocks)
+        const float m = blockReduceMax(d.solver == SOLVER_FWAVE ? blockEdgeSpeed<SOLVER_FWAVE>(d, B, cur)
+                                                                : blockEdgeSpeed<SOLVER_HLLE>(d, B, cur),
+                                       sRed);
+        if (t == 0) {
+            G->speed = m;
+            G->dt = ltsRoundTimestep(L, C, timestepFromSpeed(m, B.dx, B.dy, d.semantics));
+            if (!(m == m)) G->status |= 1;  // NaN wave speed
+        }
+        __syncthreads();
     }
     // the block's state back to global memory (read by the next kernels
     // only); the last CTA lists the enabled blocks (update pass) and those at
     // the start of their interval (speed pass) from what thread 0 wrote
     // before its release; the others take Tsync / stepSize, the step the
     // speed pass would round to (SWE_Block::getRoundTimestep)
-    __syncthreads();
     if (running && t < kLInts) reinterpret_cast<int *>(d.lts + k)[t] = reinterpret_cast<const int *>(&L)[t];
     if (t == 0)
         sLast = arriveAcqRel(reinterpret_cast<unsigned *>(d.ltsWork + kLwArrCheck), 1u) + 1u == gridDim.x;
@@ -262,7 +328,7 @@ __global__ void ltsCheckKernel(const DomainDev d) {
             step = __ldcg(&d.groups[j].ltsStep);
             pairs = ((Bj.ny + TY - 1) / TY) * Bj.nx;
             upd = en != 0;
-            spd = upd && step == 0;
+            spd = upd && step == 0 && !d.ltsCheckSpeed;  // (else the check set its dt)
         };
         int v[4] = {0, 0, 0, 0};  // enabled blocks, their pairs, interval starts, their pairs
         constexpr int kCache = 4;  // the first entries' values, kept for the second pass
@@ -284,7 +350,7 @@ __global__ void ltsCheckKernel(const DomainDev d) {
             if (spd) {
                 v[2]++;
                 v[3] += pairs;
-            } else if (upd) {
+            } else if (upd && step != 0) {
                 d.groups[j].dt = C.maxTimestepLocal / float(step);
             }
         }

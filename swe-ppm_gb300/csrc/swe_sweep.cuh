@@ -487,7 +487,9 @@ __global__ void __launch_bounds__(kMaxTileRows, 4) sweepKernel(const DomainDev d
     // one segment: rows [wu.y0, wu.y0 + TY) x columns [wu.x0, wu.x1) of a block
     auto segment = [&](const WorkUnit wu, unsigned count, unsigned total) {
         const BlockDesc B = d.blocks[wu.block];
-        GroupState *G = d.groups + B.group;
+        // local time stepping: block k is dt group k, so the group's loads
+        // need not wait for the block descriptor's
+        GroupState *G = d.groups + (d.ltsWork ? wu.block : B.group);
         if (!groupActive(G)) return;
         const int cur = __ldg(&G->cur);
         const float *__restrict__ H = pick(d.h, cur) + B.base;

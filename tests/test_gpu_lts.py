@@ -52,6 +52,17 @@ def test_lts_full_speed_pass_and_uneven_blocks(swe, oracle_mod):
     assert_bitwise(hv, ref[2], "hv")
 
 
+@pytest.mark.parametrize("name", ["hlle", "fwave"])
+def test_lts_blocks_above_the_check_speed_size(swe, oracle_mod, name):
+    """f-wave / HLLE blocks of 144^2 cells, above the 128^2 up to which the
+    check kernel runs an interval start's speed pass itself: these take the
+    separate speed launch (the smaller blocks of the other tests the check)."""
+    (h, hu, hv, _), ref = run_pair(swe, oracle_mod, SOLVERS[name], 288, 288, 4, 1.0, 40.0, 2)
+    assert_bitwise(h, ref[0], "h")
+    assert_bitwise(hu, ref[1], "hu")
+    assert_bitwise(hv, ref[2], "hv")
+
+
 def test_lts_three_levels_and_half_second_intervals(swe, oracle_mod):
     """Blocks at 8, 4 and 2 steps per interval over the shoreline ramp, and
     an interval of 0.5 (the reference rounds with the absolute dt; its rounding
