@@ -129,8 +129,10 @@ template <int S> __device__ float blockEdgeSpeed(const DomainDev &d, const Block
 __global__ void ltsCheckKernel(const DomainDev d) {
     __shared__ int sAction[4], sRecv[4];  // per side: 0 none, 1 copy, 2 interpolate; layer received now
     __shared__ float sFactor[4];
-    __shared__ float sNbrLocal[4];  // per side within the rank: the neighbour's total local time
-    __shared__ int sNbrCur[4];      // and its current buffer
+    __shared__ float sNbrLocal[4];  // per side within the rank: the neighbour's total local time,
+    __shared__ int sNbrCur[4];      // its current buffer
+    __shared__ long long sNbrOff[4];  // and its copy layer: cell of position p at sNbrOff + p sNbrStride
+    __shared__ int sNbrStride[4];
     __shared__ int sLast;
     __shared__ int sScan[4][kLtsCheckThreads / 32];
     __shared__ LtsBlock L;   // the block's state, staged: its reads and writes stay on chip
@@ -159,9 +161,15 @@ __global__ void ltsCheckKernel(const DomainDev d) {
         // single array keeps them, so they are carried over first
         sStale = G->ringStale;
     } else if (t >= 32 && t < 36 && B.bnd[t - 32] == CONNECT_WITHIN_RANK) {
-        const int n = B.nbr[t - 32];
-        sNbrLocal[t - 32] = __ldcg(&d.ltsLocal[n]);
-        sNbrCur[t - 32] = __ldcg(&d.groups[n].cur);
+        const int s = t - 32, n = B.nbr[s];
+        sNbrLocal[s] = __ldcg(&d.ltsLocal[n]);
+        sNbrCur[s] = __ldcg(&d.groups[n].cur);
+        // the neighbour's copy layer: LEFT its column nx, RIGHT its column 1,
+        // BOTTOM its row ny, TOP its row 1
+        const BlockDesc &N = d.blocks[n];
+        const long long P = N.pitch;
+        sNbrOff[s] = N.base + (s == 0 ? N.nx * P : s == 1 ? P : s == 2 ? N.ny : 1);
+        sNbrStride[s] = s < 2 ? 1 : N.pitch;
     }
     __syncthreads();
     const int cur = sCur;
@@ -219,46 +227,50 @@ __global__ void ltsCheckKernel(const DomainDev d) {
             perimeterIndex(B, i, side, pos);
             ghostCell(B, side, pos, gx, gy, sx, sy);
             const size_t og = size_t(gx) * P + gy;
-            float g[3];  // the ghost's value now
-            for (int f = 0; f < 3; f++) g[f] = stale ? Fo[f][og] : F[f][og];
+            // where the ghost's new value comes from: the cell inside (wall,
+            // outflow), the neighbour's copy layer received now, or the
+            // receive ring (a layer kept from an earlier exchange); its loads
+            // go out together with the ghost's own
+            const int type = B.bnd[side];
+            const bool inside = running && (type == WALL || type == OUTFLOW);
+            const bool recv = running && !inside && sRecv[side];
+            const int a = (running && !inside) ? sAction[side] : 0;
+            const long long r = ringOffset(B, side, pos);
+            const float *src[3] = {nullptr, nullptr, nullptr};
+            size_t so = 0;
+            if (inside) {
+                for (int f = 0; f < 3; f++) src[f] = F[f];
+                so = size_t(sx) * P + sy;
+            } else if (recv) {
+                const int ncur = sNbrCur[side];
+                src[0] = pick(d.h, ncur);
+                src[1] = pick(d.hu, ncur);
+                src[2] = pick(d.hv, ncur);
+                so = size_t(sNbrOff[side] + (long long)pos * sNbrStride[side]);
+            } else if (a) {
+                for (int f = 0; f < 3; f++) src[f] = d.ring[f];
+                so = size_t(r);
+            }
+            // the ghost's value now is needed to interpolate and to carry the
+            // ring over; walls, outflow and copied layers replace it
+            float g[3] = {0.f, 0.f, 0.f}, v[3];
+            if (a == 2 || (stale && !inside && a == 0))
+                for (int f = 0; f < 3; f++) g[f] = stale ? Fo[f][og] : F[f][og];
+            if (src[0])
+                for (int f = 0; f < 3; f++) v[f] = src[f][so];
             bool changed = stale;
-            if (running) {
-                const int type = B.bnd[side];
-                if (type == WALL || type == OUTFLOW) {
-                    // walls negate the normal momentum
-                    const int negate = type == WALL ? (side < 2 ? 1 : 2) : -1;
-                    for (int f = 0; f < 3; f++) {
-                        const float v = F[f][size_t(sx) * P + sy];
-                        g[f] = (negate == f) ? -v : v;
-                    }
+            if (inside) {
+                // walls negate the normal momentum
+                const int negate = type == WALL ? (side < 2 ? 1 : 2) : -1;
+                for (int f = 0; f < 3; f++) g[f] = (negate == f) ? -v[f] : v[f];
+                changed = true;
+            } else {
+                if (recv)
+                    for (int f = 0; f < 3; f++) d.ring[f][r] = v[f];
+                if (a) {
+                    const float factor = sFactor[side];
+                    for (int f = 0; f < 3; f++) g[f] = (a == 1) ? v[f] : g[f] + (v[f] - g[f]) * factor;
                     changed = true;
-                } else {
-                    const long long r = ringOffset(B, side, pos);
-                    float v[3];
-                    if (sRecv[side]) {
-                        const BlockDesc &N = d.blocks[B.nbr[side]];
-                        const int ncur = sNbrCur[side];
-                        int nx = sx, ny = sy;  // the neighbour's copy layer
-                        switch (side) {
-                        case 0: nx = N.nx; break;
-                        case 1: nx = 1; break;
-                        case 2: ny = N.ny; break;
-                        default: ny = 1; break;
-                        }
-                        const size_t o = size_t(N.base) + size_t(nx) * size_t(N.pitch) + size_t(ny);
-                        v[0] = pick(d.h, ncur)[o];
-                        v[1] = pick(d.hu, ncur)[o];
-                        v[2] = pick(d.hv, ncur)[o];
-                        for (int f = 0; f < 3; f++) d.ring[f][r] = v[f];
-                    }
-                    const int a = sAction[side];
-                    if (a) {
-                        if (!sRecv[side])
-                            for (int f = 0; f < 3; f++) v[f] = d.ring[f][r];
-                        const float factor = sFactor[side];
-                        for (int f = 0; f < 3; f++) g[f] = (a == 1) ? v[f] : g[f] + (v[f] - g[f]) * factor;
-                        changed = true;
-                    }
                 }
             }
             if (changed)
