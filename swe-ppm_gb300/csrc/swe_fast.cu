@@ -611,13 +611,10 @@ __global__ void __launch_bounds__(kMaxTileRows / (2 * NP), MINB) fastStepKernel(
 
         // one column x = x0-1+k: XCOL its x-edges (x-1 | x), YCOL its y-edges,
         // UPD the update of column x-1, RIMX column x-1 may be on the block's
-        // left or right rim, FULL every thread has R rows in the tile (no
-        // masks).  False: a copy did not arrive in time.
-        auto column = [&](int k, auto xcolT, auto ycolT, auto updT, auto rimxT, auto fullT) -> bool {
+        // left or right rim.  False: a copy did not arrive in time.
+        auto column = [&](int k, auto xcolT, auto ycolT, auto updT, auto rimxT) -> bool {
             constexpr bool XCOL = decltype(xcolT)::value, YCOL = decltype(ycolT)::value;
             constexpr bool UPD = decltype(updT)::value, RIMX = decltype(rimxT)::value;
-            constexpr bool FULL = decltype(fullT)::value;
-            const int nA = FULL ? R : nAct;
             // wait for the strip (bounded; a stalled copy aborts the CTA)
             {
                 const unsigned a = smemAddr(&mbar[slot]);
@@ -764,11 +761,11 @@ __global__ void __launch_bounds__(kMaxTileRows / (2 * NP), MINB) fastStepKernel(
                     hn[q] = sub2(px[q].h, fma2(dtdx, add2(pendH[q], aLx[q]), mul2(dtdy, syH[q])));
                     hun[q] = sub2(px[q].hn, mul2(dtdx, add2(pendHU[q], auLx[q])));
                     hvn[q] = sub2(oldHV[q], mul2(dtdy, syHV[q]));
-                    if (FULL) {
+                    if (fullTile) {
                         hsum = add2(hsum, hn[q]);
                     } else {
-                        hsum.x += 2 * q < nA ? hn[q].x : 0.f;
-                        hsum.y += 2 * q + 1 < nA ? hn[q].y : 0.f;
+                        hsum.x += 2 * q < nAct ? hn[q].x : 0.f;
+                        hsum.y += 2 * q + 1 < nAct ? hn[q].y : 0.f;
                     }
                     hun[q].x = (hn[q].x < 0.1f) ? 0.f : hun[q].x;
                     hvn[q].x = (hn[q].x < 0.1f) ? 0.f : hvn[q].x;
@@ -778,14 +775,14 @@ __global__ void __launch_bounds__(kMaxTileRows / (2 * NP), MINB) fastStepKernel(
                     hn[q].y = fmaxf(hn[q].y, 0.f);
                 }
                 const unsigned o = unsigned(xc) * P + unsigned(yA);
-                if (FULL) {
+                if (fullTile) {
                     storeRows<NP>(HO + o, hn);
                     storeRows<NP>(HUO + o, hun);
                     storeRows<NP>(HVO + o, hvn);
                 } else {
 #pragma unroll
                     for (int r = 0; r < R; r++)
-                        if (r < nA) {
+                        if (r < nAct) {
                             HO[o + r] = lanePick(hn[r / 2], r & 1);
                             HUO[o + r] = lanePick(hun[r / 2], r & 1);
                             HVO[o + r] = lanePick(hvn[r / 2], r & 1);
@@ -802,12 +799,12 @@ __global__ void __launch_bounds__(kMaxTileRows / (2 * NP), MINB) fastStepKernel(
                         const float2 vmax = make_float2(fmaxf(fabsf(hun[q].x), fabsf(hvn[q].x)),
                                                         fmaxf(fabsf(hun[q].y), fabsf(hvn[q].y)));
                         const float2 w = fma2(vmax, mul2(rn[q], rn[q]), mul2(pk(kSqrtG), mul2(hn[q], rn[q])));
-                        if (FULL) {
+                        if (fullTile) {
                             wmax = fmaxf(wmax, fmaxf(w.x, w.y));
                             hmax = fmaxf(hmax, fmaxf(hn[q].x, hn[q].y));
                         } else {
-                            wmax = fmaxf(wmax, fmaxf(2 * q < nA ? w.x : 0.f, 2 * q + 1 < nA ? w.y : 0.f));
-                            hmax = fmaxf(hmax, fmaxf(2 * q < nA ? hn[q].x : 0.f, 2 * q + 1 < nA ? hn[q].y : 0.f));
+                            wmax = fmaxf(wmax, fmaxf(2 * q < nAct ? w.x : 0.f, 2 * q + 1 < nAct ? w.y : 0.f));
+                            hmax = fmaxf(hmax, fmaxf(2 * q < nAct ? hn[q].x : 0.f, 2 * q + 1 < nAct ? hn[q].y : 0.f));
                         }
                     }
                 } else {
@@ -847,9 +844,9 @@ __global__ void __launch_bounds__(kMaxTileRows / (2 * NP), MINB) fastStepKernel(
                         }
                     }
 #pragma unroll
-                    for (int r = 0; r < R; r++) smax = fmaxf(smax, (r < nA && k >= 3) ? sp[r] : 0.f);
+                    for (int r = 0; r < R; r++) smax = fmaxf(smax, (r < nAct && k >= 3) ? sp[r] : 0.f);
 #pragma unroll
-                    for (int r = 0; r + 1 < R; r++) smax = fmaxf(smax, (r + 1 < nA) ? sp[R + r] : 0.f);
+                    for (int r = 0; r + 1 < R; r++) smax = fmaxf(smax, (r + 1 < nAct) ? sp[R + r] : 0.f);
                     smax = fmaxf(smax, nuIn ? sp[2 * R] : 0.f);
 #pragma unroll
                     for (int r = 0; r < R; r++) nprev[r] = nxv[r];
@@ -858,7 +855,7 @@ __global__ void __launch_bounds__(kMaxTileRows / (2 * NP), MINB) fastStepKernel(
                 if (RIMX && (xc == 1 || xc == nx)) {
 #pragma unroll
                     for (int r = 0; r < R; r++)
-                        if (r < nA)
+                        if (r < nAct)
                             smax = fmaxf(smax, rimCell<S>(pick(f.d.h, cur ^ 1), pick(f.d.hu, cur ^ 1), pick(f.d.hv, cur ^ 1),
                                                           Hin, HUin, HVin, f.d.blocks, wu.block, xc, yA + r,
                                                           lanePick(hn[r / 2], r & 1), lanePick(hun[r / 2], r & 1),
@@ -906,18 +903,12 @@ __global__ void __launch_bounds__(kMaxTileRows / (2 * NP), MINB) fastStepKernel(
             return true;
         };
 
-        auto sweep = [&](auto fullT) {
-            bool ok = column(0, F_{}, F_{}, F_{}, F_{}, fullT) && column(1, T_{}, T_{}, F_{}, F_{}, fullT);
-            if (ok && XC >= 2) {
-                ok = column(2, T_{}, T_{}, T_{}, T_{}, fullT);
-                for (int k = 3; ok && k <= XC; ++k) ok = column(k, T_{}, T_{}, T_{}, F_{}, fullT);
-            }
-            if (ok) column(XC + 1, T_{}, F_{}, T_{}, T_{}, fullT);
-        };
-        if (fullTile)
-            sweep(T_{});
-        else
-            sweep(F_{});
+        bool ok = column(0, F_{}, F_{}, F_{}, F_{}) && column(1, T_{}, T_{}, F_{}, F_{});
+        if (ok && XC >= 2) {
+            ok = column(2, T_{}, T_{}, T_{}, T_{});
+            for (int k = 3; ok && k <= XC; ++k) ok = column(k, T_{}, T_{}, T_{}, F_{});
+        }
+        if (ok) ok = column(XC + 1, T_{}, F_{}, T_{}, T_{});
         if (!EDGES) smax = fmaxf(smax, hmax >= kDryTol ? wmax : 0.f);
         const bool bad = !(fabsf(hsum.x + hsum.y) <= FLT_MAX);
         __syncthreads();  // every warp's sweep is done: its stores are visible to the CTA
