@@ -2,8 +2,9 @@
 // and interval bookkeeping of SWE_Block (src/blocks/SWE_Block.hh:311-562) and
 // the overdecomposed driver's inner loop (src/examples/swe_mpi_overdecomp.cpp:266-343).
 //
-// Every block is its own dt group.  One inner iteration is three launches,
-// all decided on the device so that iterations can be replayed from a graph:
+// Every block is its own dt group.  One inner iteration is three launches
+// (two where the check runs the speed pass, below), all decided on the
+// device so that iterations can be replayed from a graph:
 //   ltsCheckKernel  one CTA per block: boundary conditions of the block and,
 //                   for each side connected to a neighbour that is
 //                   receivable, the neighbour's copy layer into the block's
@@ -22,8 +23,9 @@
 //   speed pass      the blocks at the start of an interval: maxTimestep
 //                   rounded to Tsync / 2^k (within an interval the step does
 //                   not depend on the wave speed)
-//   update pass     the enabled blocks (ghost ring carried into the new
-//                   buffer); its last CTA ends the iteration: every block at
+//   update pass     the enabled blocks (no ghost pushes: the next check
+//                   carries the ring into the new buffer); its last CTA ends
+//                   the iteration: every block at
 //                   its interval end means t += Tsync, counters reset, and
 //                   every block's total local time is published for the next
 //                   exchange (neighbours read it while their own check runs)
