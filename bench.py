@@ -815,7 +815,9 @@ def ensemble_surrogate_measure(swe, m, device, stream, steps=10, err_steps=100, 
     the single-domain rates (CUDA events, `steps` steps after 3 warm-up
     steps).  Accuracy: after err_steps steps (each instance at its own dt),
     the relative L1 distance of h to the augmented solver's batched run,
-    largest and median over the instances."""
+    largest and median over the instances, and for the four smallest
+    instances the relative L1 and L-infinity distances to the FP64 oracle's
+    augmented solver after the same steps."""
     import torch
     inst, states = swe.dam_break_ensemble(count, seed=SEED)
     cells = float(sum(nx * ny for nx, ny, *_ in inst))
@@ -863,11 +865,31 @@ def ensemble_surrogate_measure(swe, m, device, stream, steps=10, err_steps=100, 
         a = h["augmented"][offs[k]:offs[k + 1]].reshape(nx + 2, ny + 2)[1:-1, 1:-1]
         b_ = h["surrogate"][offs[k]:offs[k + 1]].reshape(nx + 2, ny + 2)[1:-1, 1:-1]
         rel.append(float(np.abs(b_ - a).sum() / np.abs(a).sum()))
+    import oracle
+    oracle.build()
+    fp64 = {"surrogate": [], "augmented": []}
+    small = sorted(range(len(inst)), key=lambda k: inst[k][0] * inst[k][1])[:4]
+    for k in small:
+        nx, ny, dx, dy, bnd = inst[k]
+        R = oracle.Domain([nx], [ny], dx, dy, outer=bnd, solver=oracle.AUGRIE, precision=64)
+        R.set_state(*states[k])
+        R.bathymetry_ghosts()
+        R.step(err_steps)
+        ref = R.get_state(np.float64)[0].reshape(nx + 2, ny + 2)[1:-1, 1:-1]
+        for name in fp64:
+            g = h[name][offs[k]:offs[k + 1]].reshape(nx + 2, ny + 2)[1:-1, 1:-1]
+            fp64[name].append((float(np.abs(g - ref).sum() / np.abs(ref).sum()),
+                               float(np.abs(g - ref).max() / np.abs(ref).max())))
     return {"workload": "%d radial dam breaks, nx, ny in 64..1024, augmented solver, unsplit, own dt each" % count,
             "unit": "cell-updates/s (sum over instances)", "cells": int(cells), "rates": rates,
             "speedup_vs_augmented_ensemble_step": rates["surrogate_ensemble_step"] / rates["augmented_ensemble_step"],
             "surrogate_edge_fraction": used / nedges, "error_steps": err_steps,
             "rel_l1_h_vs_augmented_max": max(rel), "rel_l1_h_vs_augmented_median": float(np.median(rel)),
+            "fp64_smallest4": {"instances": [list(inst[k][:2]) for k in small], "steps": err_steps,
+                               "rel_l1_h_surrogate_max": max(e[0] for e in fp64["surrogate"]),
+                               "rel_linf_h_surrogate_max": max(e[1] for e in fp64["surrogate"]),
+                               "rel_l1_h_augmented_max": max(e[0] for e in fp64["augmented"]),
+                               "rel_linf_h_augmented_max": max(e[1] for e in fp64["augmented"])},
             "device_status": status}
 
 
