@@ -462,7 +462,7 @@ int enqueueStep(swe_gpu_domain *D) {
 /// (unless the check runs it, DomainDev::ltsCheckSpeed), update pass of the
 /// enabled blocks (with the iteration's end)
 int enqueueLtsIteration(swe_gpu_domain *D) {
-    CUDA_TRY(launchLtsCheck(D->dev, D->stream));
+    CUDA_TRY(launchLtsCheck(D->dev, D->stream, !D->dev.ltsCheckSpeed));
     D->launches++;
     if (!D->dev.ltsCheckSpeed) {  // (else the check computed the interval starts' dt)
         int rc = enqueueSpeed(D);
@@ -1591,7 +1591,7 @@ int swe_gpu_lts_advance(swe_gpu_domain *dom, float t_end, int max_iterations, in
     }
     // the update passes push no ghosts: a check with the run over carries the
     // last ring into the current buffer, as the reference's single array holds it
-    CUDA_TRY(launchLtsCheck(dom->dev, dom->stream));
+    CUDA_TRY(launchLtsCheck(dom->dev, dom->stream, false));
     dom->launches++;
     // stop: no kernel runs until the next call sets a new target
     const float stop = -INFINITY;

@@ -127,7 +127,10 @@ template <int S> __device__ float blockEdgeSpeed(const DomainDev &d, const Block
 }
 
 /// exchangeGhosts + checkAllGhostlayers (src/blocks/SWE_Block.hh:375-436):
-/// one CTA per block; the last CTA lists the iteration's work
+/// one CTA per block, or with a grid of two per block (large blocks) a
+/// second CTA that takes the BOTTOM and TOP sides of the perimeter, whose
+/// ghosts and copy layers lie one pitch apart per position; the last of the
+/// blocks' first CTAs lists the iteration's work
 __global__ void ltsCheckKernel(const DomainDev d) {
     __shared__ int sAction[4], sRecv[4];  // per side: 0 none, 1 copy, 2 interpolate; layer received now
     __shared__ float sFactor[4];
@@ -143,7 +146,9 @@ __global__ void ltsCheckKernel(const DomainDev d) {
     static_assert(sizeof(LtsBlock) % 4 == 0 && sizeof(LtsBlock) / 4 + 2 <= 32, "staging by warp 0");
     static_assert(kLtsCheckThreads % 32 == 0 && kLtsCheckThreads <= 1024, "warp scan");
     pdlWaitAndRelease();
-    const int k = blockIdx.x, t = threadIdx.x;
+    const bool split = int(gridDim.x) == 2 * d.nblocks;
+    const int k = split ? int(blockIdx.x >> 1) : int(blockIdx.x), t = threadIdx.x;
+    const bool rows = split && (blockIdx.x & 1);  // the second CTA: BOTTOM and TOP only
     GroupState *G = d.groups + k;
     const LtsControl C = *d.ltsCtl;
     const bool running = ltsRunning(C);
@@ -218,13 +223,15 @@ __global__ void ltsCheckKernel(const DomainDev d) {
         // positions and store them after, so both loads are in flight at once
         float cv[3];
         size_t cog = 0;
-        if (t < 4) {
+        const bool corners = t < 4 && !rows;
+        if (corners) {
             const int gx = (t & 1) ? B.nx + 1 : 0, gy = (t & 2) ? B.ny + 1 : 0;
             const int sx = (t & 1) ? B.nx : 1, sy = (t & 2) ? B.ny : 1;
             cog = size_t(gx) * P + gy;
             for (int f = 0; f < 3; f++) cv[f] = running ? F[f][size_t(sx) * P + sy] : Fo[f][cog];
         }
-        for (int i = t; i < 2 * B.ny + 2 * B.nx; i += blockDim.x) {
+        const int iBegin = rows ? 2 * B.ny : 0, iEnd = split && !rows ? 2 * B.ny : 2 * B.ny + 2 * B.nx;
+        for (int i = iBegin + t; i < iEnd; i += blockDim.x) {
             int side, pos, gx, gy, sx, sy;
             perimeterIndex(B, i, side, pos);
             ghostCell(B, side, pos, gx, gy, sx, sy);
@@ -278,12 +285,16 @@ __global__ void ltsCheckKernel(const DomainDev d) {
             if (changed)
                 for (int f = 0; f < 3; f++) F[f][og] = g[f];
         }
-        if (t < 4)
+        if (corners)
             for (int f = 0; f < 3; f++) F[f][cog] = cv[f];
         __syncthreads();
     }
+    if (rows) return;  // (the first CTA keeps the block's state and lists)
     if (t == 0) {
-        if (stale) G->ringStale = 0;
+        // the update's last CTA sets the flag of every block in the next
+        // iteration; a check of one CTA per block (also the one after the
+        // run) clears it here.  With two, the second may not have read it yet.
+        if (stale && !split) G->ringStale = 0;
         if (running) {
             for (int s = 0; s < 4; s++) {
                 const int type = B.bnd[s];
@@ -327,7 +338,7 @@ __global__ void ltsCheckKernel(const DomainDev d) {
     // speed pass would round to (SWE_Block::getRoundTimestep)
     if (running && t < kLInts) reinterpret_cast<int *>(d.lts + k)[t] = reinterpret_cast<const int *>(&L)[t];
     if (t == 0)
-        sLast = arriveAcqRel(reinterpret_cast<unsigned *>(d.ltsWork + kLwArrCheck), 1u) + 1u == gridDim.x;
+        sLast = arriveAcqRel(reinterpret_cast<unsigned *>(d.ltsWork + kLwArrCheck), 1u) + 1u == unsigned(d.nblocks);
     __syncthreads();
     if (sLast) {
         // thread i takes blocks [i c, (i+1) c); exclusive scans of the counts
@@ -431,8 +442,8 @@ __global__ void ltsCheckKernel(const DomainDev d) {
 
 } // namespace
 
-cudaError_t launchLtsCheck(const DomainDev &d, cudaStream_t s) {
-    return launchPdl(ltsCheckKernel, dim3(unsigned(d.nblocks)), dim3(kLtsCheckThreads), s, d);
+cudaError_t launchLtsCheck(const DomainDev &d, cudaStream_t s, bool split) {
+    return launchPdl(ltsCheckKernel, dim3(unsigned(d.nblocks * (split ? 2 : 1))), dim3(kLtsCheckThreads), s, d);
 }
 
 /// getRoundTimestep of a block at the start of an interval for every entry

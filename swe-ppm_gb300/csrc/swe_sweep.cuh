@@ -240,6 +240,9 @@ __device__ __forceinline__ void ltsEndIteration(const DomainDev &d) {
     }
     done = __syncthreads_and(done);
     for (int j = 0, k = threadIdx.x; k < d.nblocks; j++, k += blockDim.x) {
+        // the blocks that stepped flipped their buffers: the next check
+        // carries their ghost ring over; the others' rings are in place
+        d.groups[k].ringStale = d.groups[k].enabled ? 1 : 0;
         int4 r, c;
         if (j < kCache) {
             c = cnt[j];
