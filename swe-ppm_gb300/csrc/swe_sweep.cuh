@@ -620,7 +620,7 @@ __global__ void __launch_bounds__(kMaxTileRows, 4) sweepKernel(const DomainDev d
                             hvn = oldHV - dtdx * syHV;
                         }
                         bad |= !(fabsf(hn) <= FLT_MAX);
-                        if (BOUNDS) {
+                        if (BOUNDS && bounds) {  // (the bounds feed only the bounded speed pass)
                             const float w = cellSpeedBound(hn, hun, hvn);
                             if (w > wmax) {
                                 wmax = w;
