@@ -462,7 +462,9 @@ int enqueueStep(swe_gpu_domain *D) {
 /// (unless the check runs it, DomainDev::ltsCheckSpeed), update pass of the
 /// enabled blocks (with the iteration's end)
 int enqueueLtsIteration(swe_gpu_domain *D) {
-    CUDA_TRY(launchLtsCheck(D->dev, D->stream, !D->dev.ltsCheckSpeed));
+    int sidePositions = 0;  // positions of a side pair (LEFT + RIGHT or BOTTOM + TOP)
+    for (const BlockDesc &B : D->blocks) sidePositions = std::max(sidePositions, 2 * std::max(B.nx, B.ny));
+    CUDA_TRY(launchLtsCheck(D->dev, D->stream, !D->dev.ltsCheckSpeed, sidePositions));
     D->launches++;
     if (!D->dev.ltsCheckSpeed) {  // (else the check computed the interval starts' dt)
         int rc = enqueueSpeed(D);

@@ -57,9 +57,10 @@ int occupancyBound(int solver);
 
 // local time stepping: exchange, ghost-layer check and interval end of one
 // inner iteration (swe_lts.cu)
-// (split: two CTAs per block, the second taking the BOTTOM and TOP sides;
-// not with the check's own speed pass, which reads the whole ring)
-cudaError_t launchLtsCheck(const DomainDev &d, cudaStream_t s, bool split);
+// (split: two CTAs per block, the second taking the BOTTOM and TOP sides,
+// of `threads` threads, the largest block's positions per CTA; not with the
+// check's own speed pass, which reads the whole ring: one CTA of 1024)
+cudaError_t launchLtsCheck(const DomainDev &d, cudaStream_t s, bool split, int threads = 0);
 // getRoundTimestep of the speed pass for a device array of time steps
 cudaError_t launchLtsRound(const float *t, int n, float tsync, int maxDivisor, int *stepSize, cudaStream_t s);
 

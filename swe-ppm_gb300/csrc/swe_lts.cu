@@ -32,6 +32,7 @@
 // Both passes split their list's (row tile, column) pairs evenly over the
 // grid.  Once t reaches the target the kernels do nothing, so a batch of
 // iterations can be queued ahead of the checkpoint.
+#include <algorithm>
 #include <cfloat>
 
 #include "swe_launch.hpp"
@@ -442,8 +443,9 @@ __global__ void ltsCheckKernel(const DomainDev d) {
 
 } // namespace
 
-cudaError_t launchLtsCheck(const DomainDev &d, cudaStream_t s, bool split) {
-    return launchPdl(ltsCheckKernel, dim3(unsigned(d.nblocks * (split ? 2 : 1))), dim3(kLtsCheckThreads), s, d);
+cudaError_t launchLtsCheck(const DomainDev &d, cudaStream_t s, bool split, int threads) {
+    threads = split ? std::min(kLtsCheckThreads, std::max(64, (threads + 31) / 32 * 32)) : kLtsCheckThreads;
+    return launchPdl(ltsCheckKernel, dim3(unsigned(d.nblocks * (split ? 2 : 1))), dim3(unsigned(threads)), s, d);
 }
 
 /// getRoundTimestep of a block at the start of an interval for every entry
