@@ -86,20 +86,23 @@ def test_lts_last_interval_reaches_duration(swe, oracle_mod):
     assert_bitwise(hv, ref[2], "hv")
 
 
-def test_lts_iteration_budget_resumes_bitwise(swe, oracle_mod):
+@pytest.mark.parametrize("solver", [4, 2], ids=["hlle_one_cta_check", "augrie_two_cta_check"])
+def test_lts_iteration_budget_resumes_bitwise(swe, oracle_mod, solver):
     """swe_gpu_lts_advance with a budget of 2 inner iterations per call: each
     call stops at the budget (graph replays queued past it do nothing) and
     carries the ghost ring into the current buffer; the next call resumes.
     Every interval takes the oracle's number of inner iterations in
     ceil(iterations / 2) calls, and two intervals run that way give the
-    oracle's step counts and state bit for bit."""
+    oracle's step counts and state bit for bit.  HLLE on these small blocks
+    checks with one CTA per block (which also runs the speed pass), the
+    augmented solver with two."""
     budget = 2
     geo, h, hu, hv, b = swe.init_domain(swe.SCENARIO_SHORELINE, 128, 96, 16, [11, 50000.0])
-    R = oracle_mod.Domain(geo["nx_cols"], geo["ny_rows"], geo["dx"], geo["dy"], outer=geo["boundary"], solver=4,
+    R = oracle_mod.Domain(geo["nx_cols"], geo["ny_rows"], geo["dx"], geo["dy"], outer=geo["boundary"], solver=solver,
                           lts_max_timestep=1.0, duration=40.0)
     R.set_state(h, hu, hv, b)
     R.bathymetry_ghosts()
-    D = swe.Domain(geo["nx_cols"], geo["ny_rows"], geo["dx"], geo["dy"], boundary=geo["boundary"], solver=4,
+    D = swe.Domain(geo["nx_cols"], geo["ny_rows"], geo["dx"], geo["dy"], boundary=geo["boundary"], solver=solver,
                    lts_max_timestep=1.0, duration=40.0)
     D.upload(h, hu, hv, b)
     D.exchange_bathymetry()
