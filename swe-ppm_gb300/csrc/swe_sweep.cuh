@@ -215,9 +215,10 @@ __device__ __forceinline__ void ltsEndIteration(const DomainDev &d) {
     LtsControl &C = *d.ltsCtl;
     const bool running = ltsRunning(C);
     // each block's ghost-layer states and counters in one load round (the
-    // first kCache blocks of a thread stay in registers between the passes)
+    // counters of a thread's first kCache blocks stay in registers between
+    // the passes)
     constexpr int kCache = 4;
-    int4 rec[kCache], cnt[kCache];  // received[4]; stepSize, stepSizeCounter, timestepCounter, notified
+    int4 cnt[kCache];  // stepSize, stepSizeCounter, timestepCounter, notified
     auto load = [&](int k, int4 &r, int4 &c) {
         const int4 *p = reinterpret_cast<const int4 *>(d.lts + k);
         r = p[0];
@@ -230,12 +231,9 @@ __device__ __forceinline__ void ltsEndIteration(const DomainDev &d) {
     };
     bool done = true;
     for (int j = 0, k = threadIdx.x; k < d.nblocks; j++, k += blockDim.x) {
-        int4 r, c;
+        int4 r, c;  // received[4]; the counters
         load(k, r, c);
-        if (j < kCache) {
-            rec[j] = r;
-            cnt[j] = c;
-        }
+        if (j < kCache) cnt[j] = c;
         if (running && !finished(r, c)) done = false;
     }
     done = __syncthreads_and(done);
